@@ -1,0 +1,10 @@
+"""GB300-native DYNAMITE hot path: 2D-interpolation renormalisation, memory-kernel
+convolutions, EOM right-hand side with r(t), adaptive RK stages and sparsify,
+as hand-written sm_103a CUDA kernels behind the C ABI of include/dyn.h."""
+from . import grid
+from ._lib import DynError, lib
+from .grid import Grid
+from .simulation import METHODS, Model, Simulation, State, StepResult, serk2_method
+
+__all__ = ["Grid", "Model", "Simulation", "State", "StepResult", "DynError", "METHODS", "grid", "lib",
+           "serk2_method"]

@@ -1,0 +1,131 @@
+"""ctypes binding of include/dyn.h (libdynamite_gb300.so, built in-tree).
+
+The library is the product: there is no Python or CPU fallback for any call
+that needs it, and loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+dp = C.POINTER(C.c_double)
+ip = C.POINTER(C.c_int)
+i64p = C.POINTER(C.c_int64)
+szp = C.POINTER(C.c_size_t)
+
+DYN_OK = 0
+DYN_RK54, DYN_SSPRK104 = 1, 2
+DYN_FP64, DYN_MIXED = 0, 1
+DYN_SEARCH_BINARY, DYN_SEARCH_LOWER_BOUND = 0, 1
+DYN_SPARSIFY_CPU, DYN_SPARSIFY_CUDA_HOST, DYN_SPARSIFY_GPU = 0, 1, 2
+DYN_RINT, DYN_POSB1X, DYN_POSB2X = 16, 17, 18
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("p", C.c_int), ("p2", C.c_int), ("lam", C.c_double), ("T0", C.c_double), ("Gamma", C.c_double),
+        ("len", C.c_size_t), ("depth", C.c_size_t), ("delta_t_min", C.c_double), ("delta_max", C.c_double),
+        ("precision", C.c_int), ("search", C.c_int), ("history_capacity", C.c_size_t), ("device", C.c_int),
+        ("stream", C.c_void_p), ("use_graph", C.c_int),
+    ]
+
+
+class Tables(C.Structure):
+    _fields_ = [
+        ("theta", dp), ("phi2", dp), ("integ", dp),
+        ("indsA1y", i64p), ("indsA2y", i64p), ("indsB2y", i64p),
+        ("weightsA1y", dp), ("weightsA2y", dp), ("weightsB2y", dp),
+    ]
+
+
+class StateC(C.Structure):
+    _fields_ = [
+        ("n", C.c_size_t), ("t1grid", dp), ("delta_t_ratio", dp), ("QK", dp), ("QR", dp), ("dQK", dp),
+        ("dQR", dp), ("rvec", dp), ("drvec", dp),
+    ]
+
+
+class Controller(C.Structure):
+    _fields_ = [("delta_t", C.c_double), ("delta", C.c_double), ("delta_old", C.c_double), ("loop", C.c_int),
+                ("method", C.c_int)]
+
+
+class StepResult(C.Structure):
+    _fields_ = [("delta", C.c_double), ("t", C.c_double), ("r", C.c_double), ("energy", C.c_double),
+                ("qk0", C.c_double), ("dr", C.c_double)]
+
+
+class RunParams(C.Structure):
+    _fields_ = [
+        ("nsteps", C.c_int), ("tmax", C.c_double), ("dt_schedule", dp), ("method_schedule", ip),
+        ("gpu_rollback", C.c_int), ("out_dt", dp), ("out_method", ip), ("out_delta", dp), ("out_t", dp),
+        ("out_energy", dp), ("out_qk0", dp), ("out_r", dp),
+    ]
+
+
+_lib = None
+
+
+class DynError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load the native library; raise if it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise DynError(f"{LIB_PATH} is missing: build it with `python -m dynamite_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        sigs = {
+            "dyn_abi_version": ([], C.c_int),
+            "dyn_last_error": ([], C.c_char_p),
+            "dyn_ctx_create": ([C.POINTER(Config), C.POINTER(Tables), C.POINTER(vp)], C.c_int),
+            "dyn_ctx_destroy": ([vp], C.c_int),
+            "dyn_sync": ([vp], C.c_int),
+            "dyn_state_init": ([vp, C.c_double], C.c_int),
+            "dyn_state_upload": ([vp, C.POINTER(StateC)], C.c_int),
+            "dyn_state_rows": ([vp, szp], C.c_int),
+            "dyn_state_download": ([vp, C.POINTER(StateC)], C.c_int),
+            "dyn_controller_get": ([vp, C.POINTER(Controller)], C.c_int),
+            "dyn_controller_set": ([vp, C.POINTER(Controller)], C.c_int),
+            "dyn_interpolate": ([vp, dp, dp], C.c_int),
+            "dyn_get_interp": ([vp, C.c_int, dp], C.c_int),
+            "dyn_qkr_step": ([vp, dp, dp], C.c_int),
+            "dyn_rhs": ([vp, dp, dp], C.c_int),
+            "dyn_rstep": ([vp, dp], C.c_int),
+            "dyn_drstep2": ([vp, dp, dp, dp, dp, C.c_double, dp], C.c_int),
+            "dyn_energy": ([vp, dp], C.c_int),
+            "dyn_conv_dev": ([vp, C.c_int, vp, vp, C.c_size_t, C.c_double, vp], C.c_int),
+            "dyn_search_dev": ([vp, vp, C.c_size_t, vp, C.c_size_t, vp], C.c_int),
+            "dyn_update": ([vp, C.c_int, C.c_double, C.POINTER(StepResult)], C.c_int),
+            "dyn_run": ([vp, C.POINTER(RunParams), C.POINTER(StepResult)], C.c_int),
+            "dyn_sparsify": ([vp, C.c_double, C.c_int, szp], C.c_int),
+            "dyn_rollback": ([vp, C.c_int], C.c_int),
+            "dyn_last_row": ([vp, dp, dp], C.c_int),
+            "dyn_profile_stage": ([vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
+            "dyn_probe_fp64": ([C.c_int, dp], C.c_int),
+            "dyn_grid_generate": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
+                                   dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
+        }
+        for name, (args, res) in sigs.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != DYN_OK:
+        msg = lib().dyn_last_error().decode(errors="replace")
+        raise DynError(f"{what} failed (status {status}): {msg}")
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(dp)

@@ -1,0 +1,981 @@
+// Host side of the GB300-native DYNAMITE hot path: the C ABI of include/dyn.h.
+//
+// The host owns what is scalar and sequential — the time grid arithmetic
+// (replicated operation by operation from the reference so that t1grid and
+// delta_t_ratio come out bit-identical), the RK tableaux, the step-size
+// controller — and keeps a mirror of t1grid/delta_t_ratio.  Everything of
+// size L or L^2 lives on the device.  One RK step is one H2D copy of the
+// stage descriptors, 2 kernels per stage, and one D2H copy of the step result,
+// optionally replayed as a CUDA graph.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/dyn.h"
+#include "dyn_kernels.cuh"
+
+using namespace dyn;
+
+namespace {
+
+thread_local std::string g_err;
+
+dyn_status fail(dyn_status s, const std::string& msg) {
+    g_err = msg;
+    return s;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(DYN_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+    } while (0)
+
+const double RMAX[11] = {3, 13, 20, 80, 180, 320, 500, 720, 980, 1280, 1620};
+
+// Dormand-Prince tableau (runge_kutta.cpp:149-159)
+const double RK54_A[7][7] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {1.0 / 5, 0, 0, 0, 0, 0, 0},
+    {3.0 / 40, 9.0 / 40, 0, 0, 0, 0, 0},
+    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0, 0},
+    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0, 0},
+    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0, 0},
+    {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84, 0}};
+const double RK54_B[7] = {35.0 / 384, 0.0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84, 0.0};
+const double RK54_B2[7] = {5179.0 / 57600, 0.0, 7571.0 / 16695, 393.0 / 640, -92097.0 / 339200, 187.0 / 2100, 1.0 / 40};
+
+// SSPRK(10,4) tableau (runge_kutta.cpp:22-35)
+double ssp_a(int r, int c) {
+    if (c >= r) return 0.0;
+    return (r <= 4 || c >= 5) ? 1.0 / 6 : 1.0 / 15;
+}
+const double SSP_B[10] = {1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10};
+const double SSP_B2[10] = {0., 2.0 / 9, 0, 0, 5.0 / 18, 1.0 / 3, 0., 0., 0., 1.0 / 6};
+
+// SERK2 coefficients (runge_kutta.cu:202-272), long double solve
+long double chebT(int n, long double x) {
+    if (n == 0) return 1.0L;
+    if (n == 1) return x;
+    long double t0 = 1.0L, t1 = x;
+    for (int i = 2; i <= n; ++i) { long double t2 = 2.0L * x * t1 - t0; t0 = t1; t1 = t2; }
+    return t1;
+}
+long double chebU(int n, long double x) {
+    if (n == 0) return 1.0L;
+    if (n == 1) return 2.0L * x;
+    long double u0 = 1.0L, u1 = 2.0L * x;
+    for (int i = 2; i <= n; ++i) { long double u2 = 2.0L * x * u1 - u0; u0 = u1; u1 = u2; }
+    return u1;
+}
+std::vector<double> serk_coeffs(int q) {
+    const int mm = 2, s = mm * q, N = s + 1;
+    const long double mup = 19.0L / 20.0L;
+    const long double a2 = (long double)q / ((long double)s * s);
+    const long double w0 = 1.0L + mup / ((long double)s * s);
+    const long double w1 = chebT(s, w0) / ((long double)s * chebU(s - 1, w0));
+    std::vector<std::vector<long double>> A(N, std::vector<long double>(N + 1, 0.0L));
+    for (int zi = 0; zi < N; ++zi) {
+        const long double z = (long double)(zi + 1);
+        A[zi][N] = chebT(s, w0 + w1 * z) / chebT(s, w0);
+        A[zi][0] = chebT(0, 1.0L + a2 * z);
+        for (int j = 1; j <= q; ++j) {
+            const long double tmj = std::pow(chebT(mm, 1.0L + a2 * z), j - 1);
+            for (int i = 1; i <= mm; ++i) A[zi][i + mm * (j - 1)] = chebT(i, 1.0L + a2 * z) * tmj;
+        }
+    }
+    for (int i = 0; i < N; ++i) {
+        int mx = i;
+        for (int k = i + 1; k < N; ++k) if (std::fabs(A[k][i]) > std::fabs(A[mx][i])) mx = k;
+        std::swap(A[i], A[mx]);
+        for (int k = i + 1; k < N; ++k) {
+            const long double f = A[k][i] / A[i][i];
+            for (int j = i; j <= N; ++j) A[k][j] -= f * A[i][j];
+        }
+    }
+    std::vector<long double> x(N);
+    for (int i = N - 1; i >= 0; --i) {
+        x[i] = A[i][N];
+        for (int j = i + 1; j < N; ++j) x[i] -= A[i][j] * x[j];
+        x[i] /= A[i][i];
+    }
+    std::vector<double> out(N);
+    for (int i = 0; i < N; ++i) out[i] = (double)x[i];
+    return out;
+}
+
+double pow_int_h(double b, int e) {
+    if (e == 0) return 1.0;
+    if (e == 1) return b;
+    if (e == 2) return b * b;
+    if (e == 3) return b * b * b;
+    if (e == 4) { double sq = b * b; return sq * sq; }
+    double r = 1.0, c = b;
+    while (e > 0) { if (e & 1) r *= c; c *= c; e >>= 1; }
+    return r;
+}
+
+template <typename T>
+dyn_status dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) return fail(DYN_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return DYN_OK;
+}
+
+struct Ctx {
+    dyn_config cfg{};
+    int L = 0, m = 0;
+    size_t L2 = 0;
+    DevCtx d{};
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    // host mirrors of the time grid
+    std::vector<double> t1, dtr;
+    size_t n = 0, cap = 0;
+    dyn_controller ctl{};
+    double specRad = 0.0;
+    // pinned staging
+    StageDev* stages_h = nullptr;
+    Slots* slots_h = nullptr;
+    double2* rhs_h = nullptr;
+    double* scratch_dev = nullptr;  // small device scratch for the exact kernels
+    std::map<int, cudaGraphExec_t> graphs;
+    std::map<int, int> warm;
+    bool interp_alloc = false;
+
+    ~Ctx() { release(); }
+
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
+
+    void release() {
+        drop_graphs();
+        void* bufs[] = {(void*)d.theta, (void*)d.phi2, (void*)d.integ, (void*)d.iA1, (void*)d.iA2, (void*)d.iB2,
+                        (void*)d.wA1, (void*)d.wA2, (void*)d.wB2, d.KR, d.dKR, d.t1grid, d.dtr, d.inv_dtr,
+                        d.rvec, d.drvec, d.posB1x, d.posB1x_saved, d.posB2x, d.posB2x_saved, d.h, d.gS,
+                        d.geS, d.gfS, d.part, d.rowval, d.epart, d.slots, d.stages, d.rhs_out, d.ip,
+                        d.rint, scratch_dev};
+        for (void* b : bufs) if (b) cudaFree(b);
+        std::memset(&d, 0, sizeof d);
+        scratch_dev = nullptr;
+        if (stages_h) cudaFreeHost(stages_h);
+        if (slots_h) cudaFreeHost(slots_h);
+        if (rhs_h) cudaFreeHost(rhs_h);
+        stages_h = nullptr; slots_h = nullptr; rhs_h = nullptr;
+        if (own_stream && st) cudaStreamDestroy(st);
+        st = nullptr;
+    }
+
+    double Df_h(double q) const {
+        return cfg.lambda * cfg.p * pow_int_h(q, cfg.p - 1) + (1 - cfg.lambda) * cfg.p2 * pow_int_h(q, cfg.p2 - 1);
+    }
+    double DDf_h(double q) const {
+        return cfg.lambda * cfg.p * (cfg.p - 1) * pow_int_h(q, cfg.p - 2) +
+               (1 - cfg.lambda) * cfg.p2 * (cfg.p2 - 1) * pow_int_h(q, cfg.p2 - 2);
+    }
+
+    dyn_status ensure_rows(size_t rows) {
+        if (rows <= cap) return DYN_OK;
+        size_t ncap = cap ? cap : 1024;
+        while (ncap < rows) ncap *= 2;
+        double2 *KR, *dKR;
+        double *t1g, *dt, *idt, *rv, *drv;
+        dyn_status s;
+        if ((s = dalloc(&KR, ncap * L)) || (s = dalloc(&dKR, ncap * L)) || (s = dalloc(&t1g, ncap)) ||
+            (s = dalloc(&dt, ncap)) || (s = dalloc(&idt, ncap)) || (s = dalloc(&rv, ncap)) || (s = dalloc(&drv, ncap)))
+            return s;
+        if (n) {
+            CK(cudaMemcpyAsync(KR, d.KR, n * L * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(dKR, d.dKR, n * L * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(t1g, d.t1grid, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(dt, d.dtr, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(idt, d.inv_dtr, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(rv, d.rvec, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(drv, d.drvec, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            CK(cudaStreamSynchronize(st));
+        }
+        for (void* b : {(void*)d.KR, (void*)d.dKR, (void*)d.t1grid, (void*)d.dtr, (void*)d.inv_dtr, (void*)d.rvec,
+                        (void*)d.drvec})
+            if (b) cudaFree(b);
+        d.KR = KR; d.dKR = dKR; d.t1grid = t1g; d.dtr = dt; d.inv_dtr = idt; d.rvec = rv; d.drvec = drv;
+        cap = ncap;
+        drop_graphs();
+        return DYN_OK;
+    }
+
+    dyn_status upload_times() {
+        std::vector<double> inv(n);
+        for (size_t k = 0; k < n; ++k) inv[k] = dtr[k] != 0.0 ? 1.0 / dtr[k] : 0.0;
+        CK(cudaMemcpyAsync(d.t1grid, t1.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d.dtr, dtr.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d.inv_dtr, inv.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        return DYN_OK;
+    }
+
+    dyn_status pos_init() {
+        CK(launch_pos_init(d, (int)n, st));
+        return DYN_OK;
+    }
+
+    int stages_of(int method) const {
+        if (method == DYN_RK54) return 7;
+        if (method == DYN_SSPRK104) return 10;
+        return 2 * (2 * (method - 2));
+    }
+
+    // Fill stages_h for one step; returns the host-side part of the error
+    // estimate (|gt - gte|) and the final time through the out-params.
+    dyn_status build_step(int method, double dt, int* S_out, double* err_t, double* T_final, double* dtr_final) {
+        const size_t n0 = n;
+        const double T0 = t1[n0 - 1];
+        const double prev = n0 >= 2 ? T0 - t1[n0 - 2] : 0.0;
+        int S;
+        std::vector<double> Tn;  // time written by stage s
+        std::memset(stages_h, 0, sizeof(StageDev) * SMAX);
+        if (method == DYN_RK54 || method == DYN_SSPRK104) {
+            const bool ssp = method == DYN_SSPRK104;
+            S = ssp ? 10 : 7;
+            auto A = [&](int r, int c) { return ssp ? ssp_a(r, c) : RK54_A[r][c]; };
+            const double* B = ssp ? SSP_B : RK54_B;
+            const double* B2 = ssp ? SSP_B2 : RK54_B2;
+            for (int s = 0; s < S; ++s) {
+                StageDev& sp = stages_h[s];
+                sp.kind = KIND_TABLEAU;
+                sp.ncoef = s + 1;
+                double gt;
+                if (s == 0) {
+                    gt = T0 + dt * A(1, 0) * 1.0;  // runge_kutta.cpp:201
+                    sp.coef[0] = dt * A(1, 0);
+                } else if (s == S - 1) {
+                    gt = T0;
+                    for (int j = 0; j < S; ++j) { gt += dt * B[j] * 1.0; sp.coef[j] = dt * B[j]; }
+                    for (int j = 0; j < S; ++j) sp.coef_e[j] = dt * B2[j];
+                } else {
+                    gt = T0;
+                    for (int j = 0; j <= s; ++j) { gt += dt * A(s + 1, j) * 1.0; sp.coef[j] = dt * A(s + 1, j); }
+                }
+                Tn.push_back(gt);
+                // SSPRK(10,4) reuses the positions of stages 2..4 at stages 5..7
+                // (runge_kutta.cpp:60-80)
+                sp.b2_save = (ssp && s >= 2 && s <= 4) ? s - 2 : -1;
+                sp.b2_reuse = (ssp && s >= 5 && s <= 7) ? s - 5 : -1;
+                const int nx = s + 1;
+                sp.pos_save = (ssp && nx >= 2 && nx <= 4) ? nx - 2 : -1;
+                sp.pos_reuse = (ssp && nx >= 5 && nx <= 7) ? nx - 5 : -1;
+                sp.nb2_save = sp.pos_save;
+                sp.nb2_reuse = sp.pos_reuse;
+            }
+            double gte = T0;
+            for (int j = 0; j < S; ++j) gte += dt * B2[j] * 1.0;
+            *err_t = std::fabs(Tn[S - 1] - gte);
+        } else {
+            const int q = 2 * (method - 2);
+            if (q < 1 || 2 * q > SMAX) return fail(DYN_ERR_INVALID, "SERK2 order out of range");
+            S = 2 * q;
+            const std::vector<double> b = serk_coeffs(q);
+            const double alpha = 1.0 / (4 * q);
+            double gt = T0, gte = T0;
+            for (int s = 0; s < S; ++s) {
+                StageDev& sp = stages_h[s];
+                sp.kind = KIND_SERK;
+                sp.serk_c = dt * alpha;
+                sp.serk_c2 = 2 * dt * alpha;
+                sp.serk_b0 = b[0];
+                sp.serk_bnext = b[s + 1];
+                sp.b2_save = sp.b2_reuse = sp.pos_save = sp.pos_reuse = sp.nb2_save = sp.nb2_reuse = -1;
+                if (s == 0) {
+                    sp.serk_mode = 0;
+                    gt = T0 + dt * alpha * 1.0;
+                } else if (s % 2 == 0) {
+                    sp.serk_mode = 1;
+                    gt += dt * alpha * 1.0;
+                } else {
+                    sp.serk_mode = 2;
+                    gt = 2 * gt - gte + 2 * dt * alpha * 1.0;
+                    gte = gt;
+                }
+                Tn.push_back(gt);
+            }
+            *err_t = std::fabs((T0 + dt) - gt);
+        }
+        for (int s = 0; s < S; ++s) {
+            StageDev& sp = stages_h[s];
+            sp.s = s;
+            sp.last = s == S - 1;
+            sp.n0 = (int)n0;
+            sp.nrows = s == 0 ? (int)n0 : (int)n0 + 1;
+            sp.nrows_next = (int)n0 + 1;
+            sp.T = s == 0 ? T0 : Tn[s - 1];
+            sp.T_next = Tn[s];
+            sp.tdiff = Tn[s] - T0;
+            sp.dtr_new = n0 >= 2 ? sp.tdiff / prev : 0.0;  // time_steps.cpp:58-67,142-149
+        }
+        *S_out = S;
+        *T_final = Tn[S - 1];
+        *dtr_final = stages_h[S - 1].dtr_new;
+        return DYN_OK;
+    }
+
+    dyn_status enqueue_step(int S) {
+        CK(cudaMemcpyAsync(d.stages, stages_h, sizeof(StageDev) * S, cudaMemcpyHostToDevice, st));
+        for (int s = 0; s < S; ++s) CK(launch_stage(d, s, st));
+        CK(cudaMemcpyAsync(slots_h, d.slots, sizeof(Slots), cudaMemcpyDeviceToHost, st));
+        return DYN_OK;
+    }
+
+    dyn_status step(int method, double dt, dyn_step_result* res) {
+        if (n == 0) return fail(DYN_ERR_STATE, "no state: call dyn_state_init or dyn_state_upload");
+        dyn_status s = ensure_rows(n + 1);
+        if (s) return s;
+        int S;
+        double err_t, Tf, dtrf;
+        if ((s = build_step(method, dt, &S, &err_t, &Tf, &dtrf))) return s;
+        if (cfg.use_graph && warm[method] > 0) {
+            auto it = graphs.find(method);
+            if (it == graphs.end()) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                dyn_status es = enqueue_step(S);
+                cudaError_t ce = cudaStreamEndCapture(st, &g);
+                if (es) return es;
+                CK(ce);
+                cudaGraphExec_t ge;
+                CK(cudaGraphInstantiate(&ge, g, 0));
+                cudaGraphDestroy(g);
+                it = graphs.emplace(method, ge).first;
+            }
+            CK(cudaGraphLaunch(it->second, st));
+        } else {
+            if ((s = enqueue_step(S))) return s;
+            warm[method]++;
+        }
+        CK(cudaStreamSynchronize(st));
+        t1.push_back(Tf);
+        dtr.push_back(dtrf);
+        n += 1;
+        if (res) {
+            res->delta = slots_h->res_err + err_t;
+            res->t = Tf;
+            res->r = slots_h->res_r;
+            res->energy = slots_h->res_energy;
+            res->qk0 = slots_h->res_qk0;
+            res->dr = slots_h->res_dr;
+        }
+        return DYN_OK;
+    }
+};
+
+Ctx* C(void* p) { return static_cast<Ctx*>(p); }
+
+}  // namespace
+
+extern "C" {
+
+int dyn_abi_version(void) { return DYN_ABI_VERSION; }
+const char* dyn_last_error(void) { return g_err.c_str(); }
+
+dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** out) {
+    if (!cfg || !tb || !out) return fail(DYN_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const size_t L = cfg->len, m = cfg->depth;
+    if (L < 4 || L > 4096 || m < 2 || m > L) return fail(DYN_ERR_INVALID, "len must be in [4, 4096] and 2 <= depth <= len");
+    if (cfg->precision != DYN_FP64) return fail(DYN_ERR_UNSUPPORTED, "precision not available in this context type");
+    if (!tb->theta || !tb->phi2 || !tb->integ || !tb->indsA1y || !tb->indsA2y || !tb->indsB2y || !tb->weightsA1y ||
+        !tb->weightsA2y || !tb->weightsB2y)
+        return fail(DYN_ERR_INVALID, "missing table");
+    for (size_t i = 1; i < L; ++i)
+        if (!(tb->theta[i] >= tb->theta[i - 1])) return fail(DYN_ERR_INVALID, "theta must be non-decreasing");
+    if (tb->theta[0] < 0.0 || tb->theta[L - 1] != 1.0) return fail(DYN_ERR_INVALID, "theta must span [0, 1]");
+    const size_t L2 = L * L;
+    std::vector<int> i32[3];
+    const int64_t* src[3] = {tb->indsA1y, tb->indsA2y, tb->indsB2y};
+    for (int k = 0; k < 3; ++k) {
+        i32[k].resize(L2);
+        for (size_t e = 0; e < L2; ++e) {
+            const int64_t v = src[k][e];
+            if (v < 0 || (size_t)v + m > L) return fail(DYN_ERR_INVALID, "stencil start out of range [0, len-depth]");
+            i32[k][e] = (int)v;
+        }
+    }
+    for (size_t e = 0; e < L2; ++e)
+        if (!(tb->phi2[e] >= 0.0 && tb->phi2[e] <= 1.0)) return fail(DYN_ERR_INVALID, "phi2 outside [0, 1]");
+    if (tb->phi2[L2 - 1] != 1.0) return fail(DYN_ERR_INVALID, "phi2 must end at 1");
+
+    Ctx* c = new Ctx();
+    c->cfg = *cfg;
+    c->L = (int)L;
+    c->m = (int)m;
+    c->L2 = L2;
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) { delete c; return fail(DYN_ERR_CUDA, cudaGetErrorString(e)); }
+    if (cfg->stream) {
+        c->st = (cudaStream_t)cfg->stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete c; return fail(DYN_ERR_CUDA, cudaGetErrorString(e)); }
+        c->own_stream = true;
+    }
+    DevCtx& d = c->d;
+    d.L = (int)L;
+    d.m = (int)m;
+    d.search = cfg->search;
+    // tile shape: targets per thread x threads per CTA (see dyn_autotune)
+    d.tpb = 64;
+    d.kpt = L >= 512 ? 4 : (L >= 256 ? 2 : 1);
+    d.nch = (int)((L + (size_t)d.tpb * d.kpt - 1) / ((size_t)d.tpb * d.kpt));
+    DModel& M = d.M;
+    M.p = cfg->p;
+    M.p2 = cfg->p2;
+    M.cA = cfg->lambda * cfg->p;
+    M.cB = (1 - cfg->lambda) * cfg->p2;
+    M.cC = cfg->lambda * cfg->p * (cfg->p - 1);
+    M.cD = (1 - cfg->lambda) * cfg->p2 * (cfg->p2 - 1);
+    M.cE = cfg->lambda * cfg->p * (cfg->p - 1) * (cfg->p - 2);
+    M.cF = (1 - cfg->lambda) * cfg->p2 * (cfg->p2 - 1) * (cfg->p2 - 2);
+    M.T0 = cfg->T0;
+    M.Gamma = cfg->Gamma;
+
+    dyn_status s;
+    const int G = (int)((L + EPI_T - 1) / EPI_T);
+    double *th, *p2, *it, *w1, *w2, *w3;
+    int *a1, *a2, *b2;
+    if ((s = dalloc(&th, L)) || (s = dalloc(&p2, L2)) || (s = dalloc(&it, L)) || (s = dalloc(&a1, L2)) ||
+        (s = dalloc(&a2, L2)) || (s = dalloc(&b2, L2)) || (s = dalloc(&w1, L2 * m)) || (s = dalloc(&w2, L2 * m)) ||
+        (s = dalloc(&w3, L2 * m)) || (s = dalloc(&d.posB1x, L)) || (s = dalloc(&d.posB1x_saved, NSAVE * L)) ||
+        (s = dalloc(&d.posB2x, L2)) || (s = dalloc(&d.posB2x_saved, NSAVE * L2)) ||
+        (s = dalloc(&d.h, (size_t)SMAX * L)) || (s = dalloc(&d.gS, L)) || (s = dalloc(&d.geS, L)) ||
+        (s = dalloc(&d.gfS, L)) || (s = dalloc(&d.part, L * (size_t)d.nch * 8)) || (s = dalloc(&d.rowval, L)) ||
+        (s = dalloc(&d.epart, (size_t)G * EP_N)) || (s = dalloc(&d.slots, 1)) || (s = dalloc(&d.stages, SMAX)) ||
+        (s = dalloc(&d.rhs_out, L)) || (s = dalloc(&d.rint, L)) || (s = dalloc(&c->scratch_dev, 4 * L + 16))) {
+        d.theta = th; d.phi2 = p2; d.integ = it; d.iA1 = a1; d.iA2 = a2; d.iB2 = b2; d.wA1 = w1; d.wA2 = w2; d.wB2 = w3;
+        delete c;
+        return s;
+    }
+    d.theta = th; d.phi2 = p2; d.integ = it; d.iA1 = a1; d.iA2 = a2; d.iB2 = b2; d.wA1 = w1; d.wA2 = w2; d.wB2 = w3;
+#define UP(dst, srcp, count) \
+    if ((e = cudaMemcpy((void*)(dst), (srcp), (count), cudaMemcpyHostToDevice)) != cudaSuccess) { delete c; return fail(DYN_ERR_CUDA, cudaGetErrorString(e)); }
+    UP(th, tb->theta, L * sizeof(double));
+    UP(p2, tb->phi2, L2 * sizeof(double));
+    UP(it, tb->integ, L * sizeof(double));
+    UP(a1, i32[0].data(), L2 * sizeof(int));
+    UP(a2, i32[1].data(), L2 * sizeof(int));
+    UP(b2, i32[2].data(), L2 * sizeof(int));
+    UP(w1, tb->weightsA1y, L2 * m * sizeof(double));
+    UP(w2, tb->weightsA2y, L2 * m * sizeof(double));
+    UP(w3, tb->weightsB2y, L2 * m * sizeof(double));
+#undef UP
+    cudaMemset(d.slots, 0, sizeof(Slots));
+    if (cudaMallocHost((void**)&c->stages_h, sizeof(StageDev) * SMAX) != cudaSuccess ||
+        cudaMallocHost((void**)&c->slots_h, sizeof(Slots)) != cudaSuccess ||
+        cudaMallocHost((void**)&c->rhs_h, sizeof(double2) * L) != cudaSuccess) {
+        delete c;
+        return fail(DYN_ERR_NOMEM, "cudaMallocHost failed");
+    }
+    c->specRad = 4 * std::sqrt(c->DDf_h(1));
+    if ((s = c->ensure_rows(cfg->history_capacity ? cfg->history_capacity : 4096))) { delete c; return s; }
+    *out = c;
+    return DYN_OK;
+}
+
+dyn_status dyn_ctx_destroy(void* p) {
+    if (!p) return DYN_OK;
+    Ctx* c = C(p);
+    cudaSetDevice(c->cfg.device);
+    cudaStreamSynchronize(c->st);
+    delete c;
+    return DYN_OK;
+}
+
+dyn_status dyn_sync(void* p) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    CK(cudaStreamSynchronize(C(p)->st));
+    return DYN_OK;
+}
+
+// initialization.cpp:204-222
+dyn_status dyn_state_init(void* p, double delta_t) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    Ctx* c = C(p);
+    const int L = c->L;
+    c->n = 1;
+    c->t1.assign(1, 0.0);
+    c->dtr.assign(1, 0.0);
+    std::vector<double2> row(L, make_double2(1.0, 1.0)), zero(L, make_double2(0.0, 0.0));
+    CK(cudaMemcpyAsync(c->d.KR, row.data(), L * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.dKR, zero.data(), L * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    const double r0 = c->cfg.Gamma + c->Df_h(1) / c->cfg.T0;
+    CK(cudaMemcpyAsync(c->d.rvec, &r0, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    dyn_status s = c->upload_times();
+    if (s) return s;
+    CK(launch_rstep_exact(c->d, 1, c->d.drvec, c->st));
+    c->ctl.delta_t = delta_t > 0 ? delta_t : c->cfg.delta_t_min;
+    c->ctl.loop = 0;
+    c->ctl.delta = 1;
+    c->ctl.delta_old = 0;
+    c->ctl.method = c->ctl.delta_t < RMAX[0] / c->specRad ? DYN_RK54 : DYN_SSPRK104;
+    if ((s = c->pos_init())) return s;
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_state_upload(void* p, const dyn_state* stt) {
+    if (!p || !stt) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    const size_t n = stt->n, L = c->L;
+    if (n < 1) return fail(DYN_ERR_INVALID, "state needs at least one row");
+    if (!stt->t1grid || !stt->delta_t_ratio || !stt->QK || !stt->QR || !stt->dQK || !stt->dQR || !stt->rvec || !stt->drvec)
+        return fail(DYN_ERR_INVALID, "missing state array");
+    for (size_t k = 0; k < n; ++k) {
+        if (!(stt->t1grid[k] >= 0.0)) return fail(DYN_ERR_INVALID, "t1grid must be non-negative");
+        if (k && !(stt->t1grid[k] >= stt->t1grid[k - 1])) return fail(DYN_ERR_INVALID, "t1grid must be non-decreasing");
+    }
+    c->drop_graphs();
+    c->n = 0;
+    dyn_status s = c->ensure_rows(n + 1);
+    if (s) return s;
+    std::vector<double2> kr(n * L), dkr(n * L);
+    for (size_t e = 0; e < n * L; ++e) {
+        kr[e] = make_double2(stt->QK[e], stt->QR[e]);
+        dkr[e] = make_double2(stt->dQK[e], stt->dQR[e]);
+    }
+    CK(cudaMemcpyAsync(c->d.KR, kr.data(), n * L * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.dKR, dkr.data(), n * L * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.rvec, stt->rvec, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.drvec, stt->drvec, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    c->n = n;
+    c->t1.assign(stt->t1grid, stt->t1grid + n);
+    c->dtr.assign(stt->delta_t_ratio, stt->delta_t_ratio + n);
+    if ((s = c->upload_times())) return s;
+    if ((s = c->pos_init())) return s;
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_state_rows(void* p, size_t* n) {
+    if (!p || !n) return fail(DYN_ERR_INVALID, "null argument");
+    *n = C(p)->n;
+    return DYN_OK;
+}
+
+dyn_status dyn_state_download(void* p, dyn_state* stt) {
+    if (!p || !stt) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    const size_t n = c->n, L = c->L;
+    if (stt->n < n) return fail(DYN_ERR_INVALID, "state buffers hold fewer rows than the history");
+    stt->n = n;
+    std::vector<double2> kr(n * L), dkr(n * L);
+    CK(cudaMemcpyAsync(kr.data(), c->d.KR, n * L * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(dkr.data(), c->d.dKR, n * L * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    if (stt->rvec) CK(cudaMemcpyAsync(stt->rvec, c->d.rvec, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    if (stt->drvec) CK(cudaMemcpyAsync(stt->drvec, c->d.drvec, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t e = 0; e < n * L; ++e) {
+        if (stt->QK) stt->QK[e] = kr[e].x;
+        if (stt->QR) stt->QR[e] = kr[e].y;
+        if (stt->dQK) stt->dQK[e] = dkr[e].x;
+        if (stt->dQR) stt->dQR[e] = dkr[e].y;
+    }
+    if (stt->t1grid) std::memcpy(stt->t1grid, c->t1.data(), n * sizeof(double));
+    if (stt->delta_t_ratio) std::memcpy(stt->delta_t_ratio, c->dtr.data(), n * sizeof(double));
+    return DYN_OK;
+}
+
+dyn_status dyn_controller_get(void* p, dyn_controller* ctl) {
+    if (!p || !ctl) return fail(DYN_ERR_INVALID, "null argument");
+    *ctl = C(p)->ctl;
+    return DYN_OK;
+}
+
+dyn_status dyn_controller_set(void* p, const dyn_controller* ctl) {
+    if (!p || !ctl) return fail(DYN_ERR_INVALID, "null argument");
+    C(p)->ctl = *ctl;
+    return DYN_OK;
+}
+
+dyn_status dyn_interpolate(void* p, const double* posB1x, const double* posB2x) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    Ctx* c = C(p);
+    if (c->n == 0) return fail(DYN_ERR_STATE, "no state");
+    if (!c->interp_alloc) {
+        dyn_status s = dalloc(&c->d.ip, 16 * c->L2);
+        if (s) return s;
+        c->interp_alloc = true;
+    }
+    double *p1 = nullptr, *p2 = nullptr;
+    if (posB1x) {
+        if (dalloc(&p1, c->L)) return DYN_ERR_NOMEM;
+        CK(cudaMemcpyAsync(p1, posB1x, c->L * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    }
+    if (posB2x) {
+        if (dalloc(&p2, c->L2)) { cudaFree(p1); return DYN_ERR_NOMEM; }
+        CK(cudaMemcpyAsync(p2, posB2x, c->L2 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    }
+    cudaError_t e = launch_interp_exact(c->d, (int)c->n, p1, p2, c->st);
+    cudaError_t e2 = cudaStreamSynchronize(c->st);
+    if (p1) cudaFree(p1);
+    if (p2) cudaFree(p2);
+    CK(e);
+    CK(e2);
+    return DYN_OK;
+}
+
+dyn_status dyn_get_interp(void* p, int which, double* out) {
+    if (!p || !out) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    const double* src;
+    size_t count;
+    if (which >= 0 && which < 16) {
+        if (!c->interp_alloc) return fail(DYN_ERR_STATE, "call dyn_interpolate first");
+        src = c->d.ip + (size_t)which * c->L2;
+        count = c->L2;
+    } else if (which == DYN_RINT) { src = c->d.rint; count = c->L; }
+    else if (which == DYN_POSB1X) { src = c->d.posB1x; count = c->L; }
+    else if (which == DYN_POSB2X) { src = c->d.posB2x; count = c->L2; }
+    else return fail(DYN_ERR_INVALID, "unknown array");
+    CK(cudaMemcpyAsync(out, src, count * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_qkr_step(void* p, double* hK, double* hR) {
+    if (!p || !hK || !hR) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (!c->interp_alloc) return fail(DYN_ERR_STATE, "call dyn_interpolate first");
+    CK(launch_qkr_exact(c->d, (int)c->n, c->d.rhs_out, c->st));
+    CK(cudaMemcpyAsync(c->rhs_h, c->d.rhs_out, c->L * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int i = 0; i < c->L; ++i) { hK[i] = c->rhs_h[i].x; hR[i] = c->rhs_h[i].y; }
+    return DYN_OK;
+}
+
+dyn_status dyn_rhs(void* p, double* hK, double* hR) {
+    if (!p || !hK || !hR) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (c->n == 0) return fail(DYN_ERR_STATE, "no state");
+    std::memset(c->stages_h, 0, sizeof(StageDev));
+    StageDev& sp = c->stages_h[0];
+    sp.kind = KIND_RHS;
+    sp.nrows = (int)c->n;
+    sp.n0 = (int)c->n;
+    sp.T = c->t1[c->n - 1];
+    sp.b2_save = NSAVE;  // keep posB2x of the current state readable
+    sp.b2_reuse = sp.pos_save = sp.pos_reuse = sp.nb2_save = sp.nb2_reuse = -1;
+    dyn_status s = c->pos_init();
+    if (s) return s;
+    CK(cudaMemcpyAsync(c->d.stages, c->stages_h, sizeof(StageDev), cudaMemcpyHostToDevice, c->st));
+    CK(launch_stage(c->d, 0, c->st));
+    CK(cudaMemcpyAsync(c->rhs_h, c->d.rhs_out, c->L * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int i = 0; i < c->L; ++i) { hK[i] = c->rhs_h[i].x; hR[i] = c->rhs_h[i].y; }
+    return DYN_OK;
+}
+
+dyn_status dyn_rstep(void* p, double* r) {
+    if (!p || !r) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    CK(launch_rstep_exact(c->d, (int)c->n, c->scratch_dev, c->st));
+    CK(cudaMemcpyAsync(r, c->scratch_dev, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_drstep2(void* p, const double* qK, const double* qR, const double* dqK, const double* dqR, double t,
+                       double* dr) {
+    if (!p || !qK || !qR || !dqK || !dqR || !dr) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    const int L = c->L;
+    double* buf = c->scratch_dev;
+    CK(cudaMemcpyAsync(buf, qK, L * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(buf + L, qR, L * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(buf + 2 * L, dqK, L * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(buf + 3 * L, dqR, L * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(launch_drstep2_exact(c->d, buf, buf + L, buf + 2 * L, buf + 3 * L, t, buf + 4 * L, c->st));
+    CK(cudaMemcpyAsync(dr, buf + 4 * L, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_energy(void* p, double* e) {
+    if (!p || !e) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    CK(launch_energy_exact(c->d, (int)c->n, c->scratch_dev, c->st));
+    CK(cudaMemcpyAsync(e, c->scratch_dev, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_conv_dev(void* p, int kind, const double* f, const double* g, size_t n, double t, double* out) {
+    if (!p || !f || !g || !out) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (n != (size_t)c->L && n != c->L2) return fail(DYN_ERR_INVALID, "n must be len or len*len");
+    CK(launch_conv_exact(c->d, kind, f, g, n, t, out, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_search_dev(void* p, const double* list, size_t nlist, const double* elem, size_t nelem, double* out) {
+    if (!p || !list || !elem || !out || nlist == 0) return fail(DYN_ERR_INVALID, "bad argument");
+    Ctx* c = C(p);
+    CK(launch_search(c->d, list, nlist, elem, nelem, out, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_update(void* p, int method, double delta_t, dyn_step_result* res) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    if (method < 1) return fail(DYN_ERR_INVALID, "unknown method");
+    if (!(delta_t > 0.0)) return fail(DYN_ERR_INVALID, "delta_t must be positive");
+    return C(p)->step(method, delta_t, res);
+}
+
+// simulation_runner.cpp:125-304 for a fixed number of iterations
+dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
+    if (!p || !rp) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    dyn_controller& k = c->ctl;
+    const double dmax = c->cfg.delta_max, dmin = c->cfg.delta_t_min;
+    dyn_step_result r{};
+    for (int it = 0; it < rp->nsteps; ++it) {
+        if (rp->tmax > 0 && c->t1[c->n - 1] >= rp->tmax) break;
+        if (rp->dt_schedule) {
+            k.delta_t = rp->dt_schedule[it];
+            k.method = rp->method_schedule ? rp->method_schedule[it] : k.method;
+        }
+        const double t = c->t1[c->n - 1] + k.delta_t;
+        if (rp->out_dt) rp->out_dt[it] = k.delta_t;
+        if (rp->out_method) rp->out_method[it] = k.method;
+        k.delta_old = k.delta;
+        dyn_status s = c->step(k.method, k.delta_t, &r);
+        if (s) return s;
+        k.delta = r.delta;
+        k.loop++;
+        if (!rp->dt_schedule) {
+            const double ratio = c->dtr[c->n - 1];
+            if (k.delta < dmax && k.loop > 5 && (k.delta < 1.1 * k.delta_old || k.delta_old < dmax / 1000) &&
+                RMAX[k.method - 1] / c->specRad > k.delta_t && ratio == 1.0) {
+                k.delta_t *= 1.01;
+            } else if (k.delta > 2 * dmax && k.delta_t > dmin) {
+                k.delta_t *= 0.9;
+            }
+            if (k.method == DYN_SSPRK104 && k.delta > dmax && RMAX[0] / c->specRad > k.delta_t) {
+                k.method = DYN_RK54;
+                k.delta_t *= 0.5;
+            }
+            if (rp->gpu_rollback && k.delta > 2 * dmax) {
+                // simulation_runner.cpp:280-304
+                const int nr = std::min(10, std::max(0, (int)c->n - 2));
+                if (nr > 0) {
+                    if ((s = dyn_rollback(p, nr))) return s;
+                }
+                k.delta_t = 0.5 * std::min(std::max(k.delta_t, dmin), RMAX[k.method - 1] / c->specRad);
+                k.method = k.method > 3 ? 2 + (2 * (k.method - 3)) / 2 : DYN_SSPRK104;
+            }
+        }
+        if (rp->out_delta) rp->out_delta[it] = k.delta;
+        if (rp->out_t) rp->out_t[it] = t;
+        if (rp->out_energy) rp->out_energy[it] = r.energy;
+        if (rp->out_qk0) rp->out_qk0[it] = r.qk0;
+        if (rp->out_r) rp->out_r[it] = r.r;
+    }
+    if (last) *last = r;
+    return DYN_OK;
+}
+
+dyn_status dyn_rollback(void* p, int nrows) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    Ctx* c = C(p);
+    if (nrows < 0 || (size_t)nrows >= c->n - 1) return fail(DYN_ERR_INVALID, "cannot roll back that many rows");
+    const size_t target = c->n - nrows;
+    c->n = target;
+    c->t1.resize(target);
+    c->dtr.resize(target);
+    c->ctl.delta_t = c->t1[target - 1] - c->t1[target - 2];
+    c->ctl.loop -= nrows;
+    dyn_status s = c->pos_init();
+    if (s) return s;
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_last_row(void* p, double* qK, double* qR) {
+    if (!p || !qK || !qR) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (c->n == 0) return fail(DYN_ERR_STATE, "no state");
+    CK(cudaMemcpyAsync(c->rhs_h, c->d.KR + (c->n - 1) * c->L, c->L * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int i = 0; i < c->L; ++i) { qK[i] = c->rhs_h[i].x; qR[i] = c->rhs_h[i].y; }
+    return DYN_OK;
+}
+
+dyn_status dyn_profile_stage(void* p, int reps, float* ms_main, float* ms_epi) {
+    if (!p || !ms_main || !ms_epi || reps < 1) return fail(DYN_ERR_INVALID, "bad argument");
+    Ctx* c = C(p);
+    if (c->n < 2) return fail(DYN_ERR_STATE, "profile needs a history of at least two rows");
+    std::memset(c->stages_h, 0, sizeof(StageDev));
+    StageDev& sp = c->stages_h[0];
+    sp.kind = KIND_RHS;
+    sp.nrows = (int)c->n;
+    sp.n0 = (int)c->n;
+    sp.T = c->t1[c->n - 1];
+    sp.b2_save = sp.b2_reuse = sp.pos_save = sp.pos_reuse = sp.nb2_save = sp.nb2_reuse = -1;
+    dyn_status s = c->pos_init();
+    if (s) return s;
+    CK(cudaMemcpyAsync(c->d.stages, c->stages_h, sizeof(StageDev), cudaMemcpyHostToDevice, c->st));
+    CK(launch_stage(c->d, 0, c->st));  // warm
+    cudaEvent_t e0, e1, e2;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventCreate(&e2));
+    float tm = 0.f, te = 0.f;
+    for (int r = 0; r < reps; ++r) {
+        float a, b;
+        CK(cudaEventRecord(e0, c->st));
+        CK(launch_main_only(c->d, 0, c->st));
+        CK(cudaEventRecord(e1, c->st));
+        CK(launch_epi_only(c->d, 0, c->st));
+        CK(cudaEventRecord(e2, c->st));
+        CK(cudaEventSynchronize(e2));
+        CK(cudaEventElapsedTime(&a, e0, e1));
+        CK(cudaEventElapsedTime(&b, e1, e2));
+        tm += a;
+        te += b;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    *ms_main = tm / reps;
+    *ms_epi = te / reps;
+    return DYN_OK;
+}
+
+dyn_status dyn_probe_fp64(int device, double* gflops) {
+    if (!gflops) return fail(DYN_ERR_INVALID, "null argument");
+    CK(cudaSetDevice(device));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    double* buf;
+    if (dalloc(&buf, 1)) return DYN_ERR_NOMEM;
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const int threads = 256, blocks = sms * 8, iters = 4096;
+    CK(launch_fp64_probe(buf, blocks, threads, 64, st));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, st));
+    CK(launch_fp64_probe(buf, blocks, threads, iters, st));
+    CK(cudaEventRecord(b, st));
+    CK(cudaEventSynchronize(b));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaStreamDestroy(st);
+    cudaFree(buf);
+    *gflops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e9;
+    return DYN_OK;
+}
+
+// sparsifyNscale / sparsifyNscaleGPU: device indicator per node, host index
+// logic of the selected variant, one device compaction pass.
+dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    if (variant < 0 || variant > 2) return fail(DYN_ERR_INVALID, "unknown sparsify variant");
+    Ctx* c = C(p);
+    const size_t n = c->n;
+    if (n_out) *n_out = n;
+    if (n < 3) return DYN_OK;
+    unsigned char* fl_d;
+    if (dalloc(&fl_d, n)) return DYN_ERR_NOMEM;
+    std::vector<unsigned char> fl(n);
+    cudaError_t e = launch_sparsify_flags(c->d, (int)n, variant, threshold, fl_d, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fl.data(), fl_d, n, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    cudaFree(fl_d);
+    CK(e);
+    std::vector<int> inds;
+    bool erased = false;
+    if (variant == 0) {
+        inds.push_back(0);
+        for (size_t i = 2; i + 1 < n; ++i) {
+            if (fl[i] & 2) erased = true; else inds.push_back((int)i);
+        }
+        inds.push_back((int)n - 1);
+        if (!erased) return DYN_OK;
+    } else if (variant == 1) {
+        int loop = 0;
+        inds.push_back(0);
+        for (size_t i = 2; i + 1 < n; ++i) {
+            if ((fl[i] & 2) && !erased) { erased = true; ++loop; }
+            else { erased = false; ++loop; inds.push_back(loop); }
+        }
+        inds.push_back((int)n - 2);
+        inds.push_back((int)n - 1);
+    } else {
+        for (size_t i = 0; i < n; ++i) if (!(fl[i] & 1) || (fl[i] & 4)) inds.push_back((int)i);
+    }
+    const int k = (int)inds.size();
+    std::vector<int> indsD(k, 0);
+    std::vector<double> tfac(k, 1.0);
+    if (variant == 0) {
+        indsD = inds;
+    } else {
+        for (int i = 0; i + 1 < k; ++i) indsD[i + 1] = inds[i] + 1;
+        for (int i = 1; i < k; ++i) {
+            const double num = c->t1[inds[i]] - c->t1[inds[i - 1]];
+            const double den = c->t1[indsD[i]] - c->t1[indsD[i] - 1];
+            tfac[i] = variant == 2 ? (den != 0.0 ? num / den : 1.0) : num / den;
+        }
+    }
+    // new buffers sized like the old capacity
+    double2 *KRn, *dKRn;
+    double *rn, *drn, *dtmp;
+    int* id;
+    dyn_status s;
+    if ((s = dalloc(&KRn, c->cap * c->L)) || (s = dalloc(&dKRn, c->cap * c->L)) || (s = dalloc(&rn, c->cap)) ||
+        (s = dalloc(&drn, c->cap)) || (s = dalloc(&id, 2 * (size_t)k)) || (s = dalloc(&dtmp, (size_t)k)))
+        return s;
+    CK(cudaMemcpyAsync(id, inds.data(), k * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(id + k, indsD.data(), k * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(dtmp, tfac.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(launch_compact(c->d, id, id + k, variant == 0 ? nullptr : dtmp, k, KRn, dKRn, rn, drn, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    cudaFree(id);
+    cudaFree(dtmp);
+    cudaFree(c->d.KR); cudaFree(c->d.dKR); cudaFree(c->d.rvec); cudaFree(c->d.drvec);
+    c->d.KR = KRn; c->d.dKR = dKRn; c->d.rvec = rn; c->d.drvec = drn;
+    c->drop_graphs();
+    // t1grid by inds; delta_t_ratio per variant (sparsify_utils.cpp:76-96, .cu:99-110)
+    std::vector<double> t1n(k), dtrn;
+    for (int i = 0; i < k; ++i) t1n[i] = c->t1[inds[i]];
+    if (variant == 0) {
+        dtrn.resize(k);
+        for (int i = 0; i < k; ++i) dtrn[i] = c->dtr[inds[i]];
+    } else {
+        dtrn = c->dtr;
+        dtrn.resize(k);
+        std::vector<double> dg(k, 0.0);
+        for (int i = 1; i < k; ++i) dg[i] = t1n[i] - t1n[i - 1];
+        for (int i = 2; i < k; ++i) dtrn[i] = dg[i] / dg[i - 1];
+    }
+    c->t1 = t1n;
+    c->dtr = dtrn;
+    c->n = k;
+    if ((s = c->upload_times())) return s;
+    if ((s = c->pos_init())) return s;
+    CK(cudaStreamSynchronize(c->st));
+    if (n_out) *n_out = c->n;
+    return DYN_OK;
+}
+
+}  // extern "C"

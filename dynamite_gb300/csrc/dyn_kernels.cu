@@ -1,0 +1,980 @@
+// CUDA kernels of the GB300-native DYNAMITE hot path (FP64 form).
+//
+// Per RK stage the whole interpolate -> Sigma -> convolution -> RHS -> RK
+// update -> r(t) chain of the reference (interpolateGPU, QKRstepGPU,
+// drstep2GPU, appendAllGPU_ptr/replaceAllGPU_ptr, rstepGPU, RK54GPU...) runs
+// as two kernels:
+//
+//   k_main (grid L x nch): every target (i, j) gathers its A1/A2/B1/B2
+//     values from the history through the stencil tables, evaluates Sigma,
+//     and accumulates the eight int.dat-weighted products of the memory
+//     integrals; nothing of size L^2 is written.
+//   k_epi (grid L/32): finishes the row reductions, forms the EOM right-hand
+//     side, the RK stage combination, writes the history row, accumulates
+//     r(t) (and dr/dt at stage 0) and computes the next stage's positions;
+//     the last CTA to finish (atomic ticket) folds the per-CTA partials.
+//
+// A second, reference-order family of kernels ("exact") materializes the 16
+// interpolation arrays and the RHS with the reference CPU build's operation
+// order (no FMA contraction) for the C-ABI calls that mirror
+// interpolateGPU/QKRstepGPU one to one.
+#include <cfloat>
+#include <cmath>
+#include "dyn_kernels.cuh"
+
+namespace dyn {
+
+// ------------------------------------------------------------------------
+// model helpers for the fused kernels
+template <int P, int P2>
+struct Sig {
+    __device__ __forceinline__ static void d12(const DModel& M, double q, double& a, double& b) {
+        Sigma<P, P2>::eval(M, q, a, b);
+    }
+    __device__ __forceinline__ static double d1(const DModel& M, double q) {
+        if constexpr (P >= 0) return fma(M.cA, ipow_c<P - 1>(q), M.cB * ipow_c<P2 - 1>(q));
+        else return fma(M.cA, ipow_r(q, M.p - 1), M.cB * ipow_r(q, M.p2 - 1));
+    }
+    __device__ __forceinline__ static double d2(const DModel& M, double q) {
+        if constexpr (P >= 0) return fma(M.cC, ipow_c<P - 2>(q), M.cD * ipow_c<P2 - 2>(q));
+        else return fma(M.cC, ipow_r(q, M.p - 2), M.cD * ipow_r(q, M.p2 - 2));
+    }
+    __device__ __forceinline__ static double d3(const DModel& M, double q) {
+        if constexpr (P >= 0) return fma(M.cE, ipow_c<P - 3>(q), M.cF * ipow_c<P2 - 3>(q));
+        else return fma(M.cE, ipow_r(q, M.p - 3), M.cF * ipow_r(q, M.p2 - 3));
+    }
+};
+
+// sum_d w[d] * x[d] for K and R together (x interleaved)
+template <int M>
+__device__ __forceinline__ double2 dot2g(const double* __restrict__ w, const double2* __restrict__ x, int m) {
+    double2 acc = make_double2(0.0, 0.0);
+    if constexpr (M > 0 && (M % 2) == 0) {
+        const double2* w2 = reinterpret_cast<const double2*>(w);
+#pragma unroll
+        for (int d = 0; d < M / 2; ++d) {
+            const double2 ww = __ldg(w2 + d);
+            const double2 xa = __ldg(x + 2 * d), xb = __ldg(x + 2 * d + 1);
+            acc.x = fma(ww.x, xa.x, acc.x);
+            acc.y = fma(ww.x, xa.y, acc.y);
+            acc.x = fma(ww.y, xb.x, acc.x);
+            acc.y = fma(ww.y, xb.y, acc.y);
+        }
+    } else {
+        for (int d = 0; d < m; ++d) {
+            const double ww = __ldg(w + d);
+            const double2 xa = __ldg(x + d);
+            acc.x = fma(ww, xa.x, acc.x);
+            acc.y = fma(ww, xa.y, acc.y);
+        }
+    }
+    return acc;
+}
+
+template <int M>
+__device__ __forceinline__ double2 dot2s(const double* __restrict__ w, const double2* x, int m) {
+    double2 acc = make_double2(0.0, 0.0);
+    if constexpr (M > 0 && (M % 2) == 0) {
+        const double2* w2 = reinterpret_cast<const double2*>(w);
+#pragma unroll
+        for (int d = 0; d < M / 2; ++d) {
+            const double2 ww = __ldg(w2 + d);
+            const double2 xa = x[2 * d], xb = x[2 * d + 1];
+            acc.x = fma(ww.x, xa.x, acc.x);
+            acc.y = fma(ww.x, xa.y, acc.y);
+            acc.x = fma(ww.y, xb.x, acc.x);
+            acc.y = fma(ww.y, xb.y, acc.y);
+        }
+    } else {
+        for (int d = 0; d < m; ++d) {
+            const double ww = __ldg(w + d);
+            const double2 xa = x[d];
+            acc.x = fma(ww, xa.x, acc.x);
+            acc.y = fma(ww, xa.y, acc.y);
+        }
+    }
+    return acc;
+}
+
+// B1 Hermite coefficients of one target row (index_vec.cu:399-441 form,
+// with the per-row division folded into c3).
+struct B1Row {
+    int F, cubic;
+    double c0, c1, c2, c3;
+};
+
+__device__ __forceinline__ B1Row b1_row(const DevCtx& c, double pos, int maxceil, int nrows) {
+    B1Row r;
+    long long F = (long long)floor(pos);
+    if (F < 1) F = 1; else if (F > maxceil) F = maxceil;
+    r.F = (int)F;
+    const double u = (double)F - pos, u2 = u * u, u3 = u2 * u;
+    r.cubic = F < nrows - 1;
+    if (r.cubic) {
+        r.c0 = 1.0 - 3.0 * u2 - 2.0 * u3;
+        r.c1 = 3.0 * u2 + 2.0 * u3;
+        r.c2 = u + 2.0 * u2 + u3;
+        r.c3 = (u2 + u3) * c.inv_dtr[F + 1];
+    } else {
+        r.c0 = 1.0 - u2;
+        r.c1 = u2;
+        r.c2 = u + u2;
+        r.c3 = 0.0;
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------------
+// k_main: fused gathers + Sigma + convolution products for one stage.
+template <int M, int K, int P, int P2>
+__global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
+    const StageDev& sp = c.stages[s];
+    const int L = c.L, tpb = blockDim.x, i = blockIdx.y;
+    const int nrows = sp.nrows;
+    const double t = sp.T;
+    const bool live = t > 0.0;
+    extern __shared__ double2 s_last[];
+    __shared__ double s_c[4];
+    __shared__ int s_bi[2];
+    __shared__ double s_red[4][8];
+
+    const double2* KRl = c.KR + (size_t)(nrows - 1) * L;
+    for (int k = threadIdx.x; k < L; k += tpb) s_last[k] = KRl[k];
+    if (threadIdx.x == 0) {
+        if (live) {
+            const B1Row r = b1_row(c, c.posB1x[i], c.slots->maxceil, nrows);
+            s_c[0] = r.c0; s_c[1] = r.c1; s_c[2] = r.c2; s_c[3] = r.c3;
+            s_bi[0] = r.F; s_bi[1] = r.cubic;
+            if (blockIdx.x == 0) {
+                // QK^{B1}[i,0] and rInt_i for the epilogue
+                const double2 x0 = c.KR[(size_t)(r.F - 1) * L], x1 = c.KR[(size_t)r.F * L];
+                const double2 d1 = c.dKR[(size_t)r.F * L];
+                double qb = r.c0 * x0.x + r.c1 * x1.x - r.c2 * d1.x;
+                double ri = r.c0 * c.rvec[r.F - 1] + r.c1 * c.rvec[r.F] - r.c2 * c.drvec[r.F];
+                if (r.cubic) {
+                    qb -= r.c3 * c.dKR[(size_t)(r.F + 1) * L].x;
+                    ri -= r.c3 * c.drvec[r.F + 1];
+                }
+                c.rowval[i] = make_double2(qb, ri);
+            }
+        } else {
+            s_bi[0] = 1; s_bi[1] = 0;
+            s_c[0] = s_c[1] = s_c[2] = s_c[3] = 0.0;
+            if (blockIdx.x == 0) c.rowval[i] = make_double2(c.KR[0].x, c.rvec[0]);
+        }
+        if (i == 0 && blockIdx.x == 0) c.slots->q0 = KRl[0].x;
+    }
+    __syncthreads();
+
+    const DModel Mo = c.M;
+    const int m = M > 0 ? M : c.m;
+    const double bc0 = s_c[0], bc1 = s_c[1], bc2 = s_c[2], bc3 = s_c[3];
+    const int F = s_bi[0], cubic1 = s_bi[1];
+    const int maxX = c.slots->maxX;
+    const double2 fill = c.KR[0];
+    const ListView lv{c.t1grid, nrows, t};
+    const double* pos2_src = sp.b2_reuse >= 0
+        ? (sp.b2_reuse == NSAVE ? c.posB2x : c.posB2x_saved + (size_t)sp.b2_reuse * L * L) : nullptr;
+    double* pos2_dst = sp.b2_save >= 0
+        ? (sp.b2_save == NSAVE ? c.posB2x : c.posB2x_saved + (size_t)sp.b2_save * L * L) : nullptr;
+
+    double acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = 0.0;
+
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+        const int j = blockIdx.x * tpb * K + kk * tpb + threadIdx.x;
+        if (j < L) {
+            const size_t ij = (size_t)i * L + j;
+            double2 a1, a2, b1, b2;
+            if (live) {
+                a1 = dot2s<M>(c.wA1 + ij * m, s_last + __ldg(c.iA1 + ij), m);
+                a2 = dot2s<M>(c.wA2 + ij * m, s_last + __ldg(c.iA2 + ij), m);
+                {
+                    const double2 x0 = __ldg(c.KR + (size_t)(F - 1) * L + j);
+                    const double2 x1 = __ldg(c.KR + (size_t)F * L + j);
+                    const double2 d1 = __ldg(c.dKR + (size_t)F * L + j);
+                    b1.x = bc0 * x0.x + bc1 * x1.x - bc2 * d1.x;
+                    b1.y = bc0 * x0.y + bc1 * x1.y - bc2 * d1.y;
+                    if (cubic1) {
+                        const double2 d2 = __ldg(c.dKR + (size_t)(F + 1) * L + j);
+                        b1.x -= bc3 * d2.x;
+                        b1.y -= bc3 * d2.y;
+                    }
+                }
+                {
+                    double pos2;
+                    if (pos2_src) pos2 = pos2_src[ij];
+                    else {
+                        pos2 = search_pos(c.search, lv, __dmul_rn(__ldg(c.phi2 + ij), t));
+                        if (pos2_dst) pos2_dst[ij] = pos2;
+                    }
+                    long long X = (long long)pos2;
+                    if (X > maxX) X = maxX;
+                    if (X < 1) X = 1;
+                    const double x = pos2 - (double)X, x2 = x * x, x3 = x2 * x;
+                    const size_t base = (size_t)(X - 1) * L + __ldg(c.iB2 + ij);
+                    const double* w = c.wB2 + ij * m;
+                    const double2 S0 = dot2g<M>(w, c.KR + base, m);
+                    const double2 S1 = dot2g<M>(w, c.KR + base + L, m);
+                    const double2 D1 = dot2g<M>(w, c.dKR + base + L, m);
+                    if (X < nrows - 1) {
+                        const double2 D2 = dot2g<M>(w, c.dKR + base + 2 * L, m);
+                        const double e0 = 1.0 - 3.0 * x2 + 2.0 * x3, e1 = x - 2.0 * x2 + x3;
+                        const double e2 = 3.0 * x2 - 2.0 * x3;
+                        const double e3 = (x3 - x2) * c.inv_dtr[X + 1];
+                        b2.x = e0 * S0.x + e1 * D1.x + e2 * S1.x + e3 * D2.x;
+                        b2.y = e0 * S0.y + e1 * D1.y + e2 * S1.y + e3 * D2.y;
+                    } else {
+                        const double e0 = 1.0 - x2, e2 = x - x2;
+                        b2.x = e0 * S0.x + x2 * S1.x + e2 * D1.x;
+                        b2.y = e0 * S0.y + x2 * S1.y + e2 * D1.y;
+                    }
+                }
+            } else {
+                a1 = a2 = b1 = b2 = fill;
+            }
+            double sKA1, dA1, sKB1, dB1, sKB2, dB2;
+            Sig<P, P2>::d12(Mo, a1.x, sKA1, dA1);
+            const double sRA1 = dA1 * a1.y;
+            const double sRA2 = Sig<P, P2>::d2(Mo, a2.x) * a2.y;
+            Sig<P, P2>::d12(Mo, b1.x, sKB1, dB1);
+            const double sRB1 = dB1 * b1.y;
+            Sig<P, P2>::d12(Mo, b2.x, sKB2, dB2);
+            const double sRB2 = dB2 * b2.y;
+            const double wj = __ldg(c.integ + j);
+            const double wRA2 = wj * sRA2, wQRA2 = wj * a2.y;
+            acc[0] = fma(wRA2, b2.x, acc[0]);            // ConvR(SigmaRA2, QKB2)
+            acc[1] = fma(wj * sRA1, b1.x, acc[1]);       // ConvA(SigmaRA1, QKB1)
+            acc[2] = fma(wj * sKA1, b1.y, acc[2]);       // ConvA(SigmaKA1, QRB1)
+            acc[3] = fma(wQRA2, sKB2, acc[3]);           // ConvR(QRA2, SigmaKB2)
+            acc[4] = fma(wj * a1.y, sKB1, acc[4]);       // ConvA(QRA1, SigmaKB1)
+            acc[5] = fma(wj * a1.x, sRB1, acc[5]);       // ConvA(QKA1, SigmaRB1)
+            acc[6] = fma(wRA2, b2.y, acc[6]);            // ConvR(SigmaRA2, QRB2)
+            acc[7] = fma(wQRA2, sRB2, acc[7]);           // ConvR(QRA2, SigmaRB2)
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double r = warp_reduce8(acc, lane);
+    if ((lane & 3) == 0) s_red[warp][warp_reduce8_index(lane)] = r;
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double v = 0.0;
+        for (int w = 0; w < (tpb >> 5); ++w) v += s_red[w][threadIdx.x];
+        c.part[((size_t)i * gridDim.x + blockIdx.x) * 8 + threadIdx.x] = v;
+    }
+}
+
+// ------------------------------------------------------------------------
+// k_epi: RHS, RK combination, history row, r(t), next positions.
+template <int P, int P2>
+__global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
+    const StageDev& sp = c.stages[s];
+    const int L = c.L, tid = threadIdx.x, i = blockIdx.x * EPI_T + tid;
+    const DModel Mo = c.M;
+    double ep[EP_N];
+#pragma unroll
+    for (int k = 0; k < EP_N; ++k) ep[k] = 0.0;
+    __shared__ int s_is_last;
+
+    if (i < L) {
+        double a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = 0.0;
+        for (int ch = 0; ch < c.nch; ++ch) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) a[k] += c.part[((size_t)i * c.nch + ch) * 8 + k];
+        }
+        const double t = sp.T, th = c.theta[i];
+        const double tA = t * th, tR = t * (1.0 - th);
+        const double2 q = c.KR[(size_t)(sp.nrows - 1) * L + i];
+        const double2 rv = c.rowval[i];
+        const double rE = c.rowval[L - 1].y;
+        const double q0 = c.slots->q0;
+        const double fac1 = Sig<P, P2>::d1(Mo, q0) / Mo.T0, fac2 = q0 / Mo.T0;
+        const double d1 = rv.x * fac1 + q.x * (-rE) + a[0] * tR + a[1] * tA + a[2] * tA;
+        const double d2 = Sig<P, P2>::d1(Mo, rv.x) * fac2 + q.y * (2.0 * Mo.Gamma) + a[3] * tR + a[4] * tA +
+                          a[5] * tA - q.x * rv.y;
+        const double2 hs = make_double2(d1 + d2 * th, (q.y * (-rE) + a[6] * tR) + (q.y * rv.y - a[7] * tR) * th);
+        c.h[(size_t)s * L + i] = hs;
+        if (sp.kind == KIND_RHS) {
+            c.rhs_out[i] = hs;
+        } else {
+            const double2 g0 = c.KR[(size_t)(sp.n0 - 1) * L + i];
+            const double2 h0 = s == 0 ? hs : c.h[i];
+            double2 g;
+            if (sp.kind == KIND_TABLEAU) {
+                g = g0;
+                for (int j = 0; j < sp.ncoef; ++j) {
+                    const double2 hj = j == s ? hs : c.h[(size_t)j * L + i];
+                    g.x = fma(hj.x, sp.coef[j], g.x);
+                    g.y = fma(hj.y, sp.coef[j], g.y);
+                }
+                if (sp.last) {
+                    double2 ge = g0;
+                    for (int j = 0; j < sp.ncoef; ++j) {
+                        const double2 hj = j == s ? hs : c.h[(size_t)j * L + i];
+                        ge.x = fma(hj.x, sp.coef_e[j], ge.x);
+                        ge.y = fma(hj.y, sp.coef_e[j], ge.y);
+                    }
+                    ep[10] = fabs(g.x - ge.x) + fabs(g.y - ge.y);
+                }
+            } else {
+                double2 ge, gf;
+                if (sp.serk_mode == 0) {
+                    g = make_double2(fma(hs.x, sp.serk_c, g0.x), fma(hs.y, sp.serk_c, g0.y));
+                    ge = g0;
+                    gf = make_double2(g0.x * sp.serk_b0, g0.y * sp.serk_b0);
+                } else {
+                    g = c.gS[i]; ge = c.geS[i]; gf = c.gfS[i];
+                    if (sp.serk_mode == 1) {
+                        g.x = fma(hs.x, sp.serk_c, g.x);
+                        g.y = fma(hs.y, sp.serk_c, g.y);
+                    } else {
+                        g.x = fma(hs.x, sp.serk_c2, 2.0 * g.x - ge.x);
+                        g.y = fma(hs.y, sp.serk_c2, 2.0 * g.y - ge.y);
+                        ge = g;
+                    }
+                }
+                if (sp.serk_bnext != 0.0) {
+                    gf.x = fma(g.x, sp.serk_bnext, gf.x);
+                    gf.y = fma(g.y, sp.serk_bnext, gf.y);
+                }
+                c.gS[i] = g; c.geS[i] = ge; c.gfS[i] = gf;
+                if (sp.last) ep[10] = fabs(gf.x - g.x) + fabs(gf.y - g.y);
+            }
+            const double w = c.integ[i];
+            if (s == 0) {
+                // drstep2 (time_steps.cu:564-639) on the step's base row and h0
+                double sk, dd;
+                Sig<P, P2>::d12(Mo, g0.x, sk, dd);
+                const double sr = dd * g0.y;
+                const double dsk = dd * h0.x;
+                const double dsr = (Sig<P, P2>::d3(Mo, g0.x) * g0.y) * h0.x + dd * h0.y;
+                const double tw = sp.T * w;
+                ep[3] = (w * sr) * g0.x;
+                ep[4] = (w * sk) * g0.y;
+                ep[5] = (tw * dsr) * g0.x;
+                ep[6] = (tw * dsk) * g0.y;
+                ep[7] = (tw * sr) * h0.x;
+                ep[8] = (tw * sk) * h0.y;
+                if (i == 0) ep[9] = (dsk * g0.x + sk * h0.x) / Mo.T0;
+            }
+            const double td = sp.tdiff;
+            c.KR[(size_t)sp.n0 * L + i] = g;
+            c.dKR[(size_t)sp.n0 * L + i] = make_double2(td * h0.x, td * h0.y);
+            // rstep (time_steps.cpp:83-92) of the new row at its time
+            const double tn = sp.T_next, tw = tn * w;
+            double sk, dd;
+            Sig<P, P2>::d12(Mo, g.x, sk, dd);
+            ep[0] = (tw * (dd * g.y)) * g.x;
+            ep[1] = (tw * sk) * g.y;
+            if (i == 0) {
+                ep[2] = (sk * g.x) / Mo.T0;
+                ep[12] = g.x;
+                ep[13] = sk;
+            }
+            // positions of the next stage
+            double pos;
+            if (sp.pos_reuse >= 0) {
+                pos = c.posB1x_saved[(size_t)sp.pos_reuse * L + i];
+            } else {
+                const ListView lv{c.t1grid, sp.nrows_next, tn};
+                pos = search_pos(c.search, lv, __dmul_rn(th, tn));
+            }
+            c.posB1x[i] = pos;
+            if (sp.pos_save >= 0) c.posB1x_saved[(size_t)sp.pos_save * L + i] = pos;
+            ep[11] = pos;
+        }
+    }
+    // one warp per CTA: fixed butterfly sums, max for positions
+#pragma unroll
+    for (int k = 0; k < EP_N; ++k) {
+        if (k == 11) {
+            double v = ep[k];
+            for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+            ep[k] = v;
+        } else {
+            ep[k] = warp_sum(ep[k]);
+        }
+    }
+    if (tid < EP_N) {
+        double v = 0.0;
+#pragma unroll
+        for (int k = 0; k < EP_N; ++k) if (k == tid) v = ep[k];
+        c.epart[(size_t)blockIdx.x * EP_N + tid] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_is_last = atomicAdd(&c.slots->counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_is_last) return;
+    __threadfence();
+
+    double tot = 0.0;
+    if (tid < EP_N) {
+        for (unsigned b = 0; b < gridDim.x; ++b) {
+            const double v = __ldcg(c.epart + (size_t)b * EP_N + tid);
+            tot = tid == 11 ? fmax(tot, v) : tot + v;
+        }
+    }
+    __shared__ double s_tot[EP_N];
+    if (tid < EP_N) s_tot[tid] = tot;
+    __syncthreads();
+    if (tid != 0) return;
+    Slots* sl = c.slots;
+    if (sp.kind != KIND_RHS) {
+        const int n0 = sp.n0;
+        const double r_new = ((Mo.Gamma + s_tot[0]) + s_tot[1]) + s_tot[2];
+        c.rvec[n0] = r_new;
+        if (s == 0)
+            sl->dr = (((((s_tot[3] + s_tot[4]) + s_tot[5]) + s_tot[6]) + s_tot[7]) + s_tot[8]) + s_tot[9];
+        c.drvec[n0] = sp.tdiff * sl->dr;
+        c.t1grid[n0] = sp.T_next;
+        c.dtr[n0] = sp.dtr_new;
+        c.inv_dtr[n0] = sp.dtr_new != 0.0 ? 1.0 / sp.dtr_new : 0.0;
+        long long mc = (long long)ceil(s_tot[11]) - 1;
+        sl->maxceil = (int)(mc < 1 ? 1 : mc);
+        int mx;
+        if (sp.nb2_reuse >= 0) {
+            mx = sl->saved_maxX[sp.nb2_reuse];
+        } else {
+            const ListView lv{c.t1grid, sp.nrows_next, sp.T_next};
+            const double p = search_pos(c.search, lv, __dmul_rn(c.phi2[(size_t)L * L - 1], sp.T_next));
+            mx = (int)(long long)(p - 0.5);
+        }
+        sl->maxX = mx;
+        if (sp.nb2_save >= 0) sl->saved_maxX[sp.nb2_save] = mx;
+        if (sp.last) {
+            sl->res_err = s_tot[10];
+            sl->res_energy = -(s_tot[1] + s_tot[13] / Mo.T0);
+            sl->res_r = r_new;
+            sl->res_qk0 = s_tot[12];
+            sl->res_dr = sl->dr;
+        }
+    }
+    sl->counter = 0;
+}
+
+// ------------------------------------------------------------------------
+// Positions of the current state (after init/upload/sparsify/rollback).
+__global__ void k_pos_init(const DevCtx c, const int nrows) {
+    const int L = c.L;
+    __shared__ double s_max[32];
+    const double T = c.t1grid[nrows - 1];
+    const ListView lv{c.t1grid, nrows, T};
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        const double p = search_pos(c.search, lv, __dmul_rn(c.theta[i], T));
+        c.posB1x[i] = p;
+        mx = fmax(mx, p);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, s_max[w]);
+        long long mc = (long long)ceil(m) - 1;
+        c.slots->maxceil = (int)(mc < 1 ? 1 : mc);
+        const double p = search_pos(c.search, lv, __dmul_rn(c.phi2[(size_t)L * L - 1], T));
+        c.slots->maxX = (int)(long long)(p - 0.5);
+        c.slots->counter = 0;
+    }
+}
+
+// ------------------------------------------------------------------------
+// Reference-order ("exact") kernels: no contraction, the C++ expression
+// order of the reference CPU build, so results on identical inputs are
+// bit-identical to the reference compiled with -ffp-contract=off.
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+__device__ __forceinline__ double ip_exact(const double* w, const double2* x, int m, int comp) {
+    double acc = 0.0;
+    for (int d = 0; d < m; ++d) acc = add(acc, mul(w[d], comp ? x[d].y : x[d].x));
+    return acc;
+}
+
+// posB1x (given or searched), Floor clamp, B2 clamp (interpolation_core.cpp:19-114)
+__global__ void k_pos_b1_exact(const DevCtx c, const int nrows, const double* pos1_given,
+                               const double* pos2_given) {
+    const int L = c.L;
+    __shared__ double s_max[32];
+    const double T = c.t1grid[nrows - 1];
+    const ListView lv{c.t1grid, nrows, T};
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        const double p = pos1_given ? pos1_given[i] : search_pos(c.search, lv, mul(c.theta[i], T));
+        c.posB1x[i] = p;
+        mx = i == 0 ? p : fmax(mx, p);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, s_max[w]);
+        long long mc = (long long)ceil(m) - 1;
+        c.slots->maxceil = (int)(mc < 1 ? 1 : mc);
+        const double p = pos2_given ? pos2_given[(size_t)L * L - 1]
+                                    : search_pos(c.search, lv, mul(c.phi2[(size_t)L * L - 1], T));
+        c.slots->maxX = (int)(long long)(p - 0.5);
+    }
+}
+
+__global__ void k_interp_exact(const DevCtx c, const int nrows, const double* pos2_given) {
+    const int L = c.L, m = c.m;
+    const size_t L2 = (size_t)L * L;
+    const double T = c.t1grid[nrows - 1];
+    const bool live = T > 0.0;
+    const ListView lv{c.t1grid, nrows, T};
+    const DModel Mo = c.M;
+    const double2* KRl = c.KR + (size_t)(nrows - 1) * L;
+    const int maxceil = c.slots->maxceil, maxX = c.slots->maxX;
+    for (size_t ij = (size_t)blockIdx.x * blockDim.x + threadIdx.x; ij < L2; ij += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(ij / L), j = (int)(ij % L);
+        double v[8];
+        double pos2 = pos2_given ? pos2_given[ij] : search_pos(c.search, lv, mul(c.phi2[ij], T));
+        c.posB2x[ij] = pos2;
+        if (!live) {
+            for (int k = 0; k < 8; k += 2) { v[k] = c.KR[0].x; v[k + 1] = c.KR[0].y; }
+        } else {
+            // A1, A2: index_vec.cpp:15-61
+            const double* w1 = c.wA1 + ij * m;
+            const double* w2 = c.wA2 + ij * m;
+            v[0] = ip_exact(w1, KRl + c.iA1[ij], m, 0);
+            v[1] = ip_exact(w1, KRl + c.iA1[ij], m, 1);
+            v[2] = ip_exact(w2, KRl + c.iA2[ij], m, 0);
+            v[3] = ip_exact(w2, KRl + c.iA2[ij], m, 1);
+            // B1: index_vec.cpp:63-136
+            {
+                const double pos = c.posB1x[i];
+                long long F = (long long)floor(pos);
+                if (F < 1) F = 1; else if (F > maxceil) F = maxceil;
+                const double wt = sub((double)F, pos);
+                const double in3 = mul(wt, wt), in4 = mul(in3, wt);
+                const double2 x0 = c.KR[(size_t)(F - 1) * L + j], x1 = c.KR[(size_t)F * L + j];
+                const double2 d1 = c.dKR[(size_t)F * L + j];
+                if (F < nrows - 1) {
+                    const double2 d2 = c.dKR[(size_t)(F + 1) * L + j];
+                    const double dr = c.dtr[F + 1];
+                    const double e0 = sub(sub(1.0, mul(3.0, in3)), mul(2.0, in4));
+                    const double e1 = add(mul(3.0, in3), mul(2.0, in4));
+                    const double e2 = add(add(wt, mul(2.0, in3)), in4);
+                    const double e3 = add(in3, in4);
+                    v[4] = sub(sub(add(mul(e0, x0.x), mul(e1, x1.x)), mul(e2, d1.x)), dvd(mul(e3, d2.x), dr));
+                    v[5] = sub(sub(add(mul(e0, x0.y), mul(e1, x1.y)), mul(e2, d1.y)), dvd(mul(e3, d2.y), dr));
+                } else {
+                    const double e0 = sub(1.0, in3), e2 = add(wt, in3);
+                    v[4] = add(sub(mul(e0, x0.x), mul(e2, d1.x)), mul(in3, x1.x));
+                    v[5] = add(sub(mul(e0, x0.y), mul(e2, d1.y)), mul(in3, x1.y));
+                }
+            }
+            // B2: index_mat.cpp:18-91
+            {
+                long long X = (long long)pos2;
+                if (X > maxX) X = maxX;
+                if (X < 1) X = 1;
+                const double x = sub(pos2, (double)X), x2 = mul(x, x), x3 = mul(x2, x);
+                const size_t base = (size_t)(X - 1) * L + c.iB2[ij];
+                const double* w = c.wB2 + ij * m;
+                for (int comp = 0; comp < 2; ++comp) {
+                    const double S0 = ip_exact(w, c.KR + base, m, comp);
+                    const double D1 = ip_exact(w, c.dKR + base + L, m, comp);
+                    const double S1 = ip_exact(w, c.KR + base + L, m, comp);
+                    double val;
+                    if (X < nrows - 1) {
+                        const double D2 = ip_exact(w, c.dKR + base + 2 * L, m, comp);
+                        const double e0 = add(sub(1.0, mul(3.0, x2)), mul(2.0, x3));
+                        const double e1 = add(sub(x, mul(2.0, x2)), x3);
+                        const double e2 = sub(mul(3.0, x2), mul(2.0, x3));
+                        const double e3 = add(-x2, x3);
+                        val = add(add(add(mul(e0, S0), mul(e1, D1)), mul(e2, S1)), dvd(mul(e3, D2), c.dtr[X + 1]));
+                    } else {
+                        val = add(add(mul(sub(1.0, x2), S0), mul(x2, S1)), mul(sub(x, x2), D1));
+                    }
+                    v[6 + comp] = val;
+                }
+            }
+        }
+        for (int k = 0; k < 8; ++k) c.ip[(size_t)k * L2 + ij] = v[k];
+        // Sigma (math_sigma.cpp:7-62): SigmaK = f'(QK), SigmaR = f''(QK) QR
+        for (int f = 0; f < 4; ++f) {
+            c.ip[(size_t)(8 + 2 * f) * L2 + ij] = Df_x(Mo, v[2 * f]);
+            c.ip[(size_t)(9 + 2 * f) * L2 + ij] = mul(DDf_x(Mo, v[2 * f]), v[2 * f + 1]);
+        }
+    }
+}
+
+// rInt: index_vec.cpp:138-156
+__global__ void k_rint_exact(const DevCtx c, const int nrows) {
+    const int L = c.L;
+    const bool live = c.t1grid[nrows - 1] > 0.0;
+    const int maxceil = c.slots->maxceil;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        if (!live) { c.rint[i] = c.rvec[0]; continue; }
+        const double pos = c.posB1x[i];
+        long long F = (long long)floor(pos);
+        if (F < 1) F = 1; else if (F > maxceil) F = maxceil;
+        const double u = sub((double)F, pos), u2 = mul(u, u), u3 = mul(u, mul(u, u));
+        double r;
+        if (F < nrows - 1) {
+            const double e0 = sub(sub(1.0, mul(3.0, u2)), mul(2.0, u3));
+            const double e1 = add(mul(3.0, u2), mul(2.0, u3));
+            const double e2 = add(add(u, mul(2.0, u2)), u3);
+            r = sub(sub(add(mul(e0, c.rvec[F - 1]), mul(e1, c.rvec[F])), mul(e2, c.drvec[F])),
+                    dvd(mul(add(u2, u3), c.drvec[F + 1]), c.dtr[F + 1]));
+        } else {
+            r = sub(add(mul(sub(1.0, u2), c.rvec[F - 1]), mul(u2, c.rvec[F])), mul(add(u, u2), c.drvec[F]));
+        }
+        c.rint[i] = r;
+    }
+}
+
+// ConvA/ConvR of one row, convolution.cpp:5-50 order
+__device__ double conv_row_exact(const DevCtx& c, const double* f, const double* g, int row) {
+    const int L = c.L;
+    double o = 0.0;
+    for (int k = 0; k < L; ++k) o = add(o, mul(mul(c.integ[k], f[(size_t)row * L + k]), g[(size_t)row * L + k]));
+    return o;
+}
+
+// QKstep / QRstep (time_steps.cpp:27-47, 94-100) on the materialized arrays
+__global__ void k_qkr_exact(const DevCtx c, const int nrows, double2* out) {
+    const int L = c.L;
+    const size_t L2 = (size_t)L * L;
+    const DModel Mo = c.M;
+    const double t = c.t1grid[nrows - 1];
+    const double* ip = c.ip;
+    const double2* q = c.KR + (size_t)(nrows - 1) * L;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        const double th = c.theta[i];
+        const double tA = mul(t, th), tR = mul(t, sub(1.0, th));
+        const double rE = c.rint[L - 1];
+        const double q0 = q[0].x;
+        const double cR1 = mul(conv_row_exact(c, ip + 11 * L2, ip + 6 * L2, i), tR);   // SigmaRA2, QKB2
+        const double cA1 = mul(conv_row_exact(c, ip + 9 * L2, ip + 4 * L2, i), tA);    // SigmaRA1, QKB1
+        const double cA2 = mul(conv_row_exact(c, ip + 8 * L2, ip + 5 * L2, i), tA);    // SigmaKA1, QRB1
+        const double cR2 = mul(conv_row_exact(c, ip + 3 * L2, ip + 14 * L2, i), tR);   // QRA2, SigmaKB2
+        const double cA3 = mul(conv_row_exact(c, ip + 1 * L2, ip + 12 * L2, i), tA);   // QRA1, SigmaKB1
+        const double cA4 = mul(conv_row_exact(c, ip + 0 * L2, ip + 13 * L2, i), tA);   // QKA1, SigmaRB1
+        const double cR3 = mul(conv_row_exact(c, ip + 11 * L2, ip + 7 * L2, i), tR);   // SigmaRA2, QRB2
+        const double cR4 = mul(conv_row_exact(c, ip + 3 * L2, ip + 15 * L2, i), tR);   // QRA2, SigmaRB2
+        const double qb = ip[4 * L2 + (size_t)i * L];
+        const double fac1 = dvd(Df_x(Mo, q0), Mo.T0);
+        const double d1 = add(add(add(add(mul(qb, fac1), mul(q[i].x, -rE)), cR1), cA1), cA2);
+        const double fac2 = dvd(q0, Mo.T0);
+        const double d2 = sub(add(add(add(add(mul(Df_x(Mo, qb), fac2), mul(q[i].y, mul(2.0, Mo.Gamma))), cR2), cA3), cA4),
+                              mul(q[i].x, c.rint[i]));
+        const double hK = add(d1, mul(d2, th));
+        const double e1 = add(mul(q[i].y, -rE), cR3);
+        const double e2 = sub(mul(q[i].y, c.rint[i]), cR4);
+        out[i] = make_double2(hK, add(e1, mul(e2, th)));
+    }
+}
+
+// rstep (time_steps.cpp:83-92), one thread, reference order
+__global__ void k_rstep_exact(const DevCtx c, const int nrows, double* out) {
+    const int L = c.L;
+    const DModel Mo = c.M;
+    const double t = c.t1grid[nrows - 1];
+    const double2* q = c.KR + (size_t)(nrows - 1) * L;
+    double A = 0.0, B = 0.0;
+    for (int j = 0; j < L; ++j) {
+        const double sk = Df_x(Mo, q[j].x), sr = mul(DDf_x(Mo, q[j].x), q[j].y);
+        A = add(A, mul(mul(mul(t, c.integ[j]), sr), q[j].x));
+        B = add(B, mul(mul(mul(t, c.integ[j]), sk), q[j].y));
+    }
+    const double sk0 = Df_x(Mo, q[0].x);
+    out[0] = add(add(add(Mo.Gamma, A), B), dvd(mul(sk0, q[0].x), Mo.T0));
+}
+
+// drstep2 (time_steps.cpp:117-125), one thread, reference order
+__global__ void k_drstep2_exact(const DevCtx c, const double* qK, const double* qR, const double* dqK,
+                                const double* dqR, const double t, double* out) {
+    const int L = c.L;
+    const DModel Mo = c.M;
+    double S[6] = {0, 0, 0, 0, 0, 0};
+    double dsk0 = 0.0, sk0 = 0.0;
+    for (int j = 0; j < L; ++j) {
+        const double q = qK[j], r = qR[j], dq = dqK[j], dr = dqR[j];
+        const double sk = Df_x(Mo, q), sr = mul(DDf_x(Mo, q), r);
+        const double dsk = add(mul(DDf_x(Mo, q), dq), mul(0.0, dr));
+        const double dsr = add(mul(mul(DDDf_x(Mo, q), r), dq), mul(DDf_x(Mo, q), dr));
+        const double w = c.integ[j], tw = mul(t, w);
+        S[0] = add(S[0], mul(mul(mul(1.0, w), sr), q));
+        S[1] = add(S[1], mul(mul(mul(1.0, w), sk), r));
+        S[2] = add(S[2], mul(mul(tw, dsr), q));
+        S[3] = add(S[3], mul(mul(tw, dsk), r));
+        S[4] = add(S[4], mul(mul(tw, sr), dq));
+        S[5] = add(S[5], mul(mul(tw, sk), dr));
+        if (j == 0) { dsk0 = dsk; sk0 = sk; }
+    }
+    const double term = dvd(add(mul(dsk0, qK[0]), mul(sk0, dqK[0])), Mo.T0);
+    out[0] = add(add(add(add(add(add(S[0], S[1]), S[2]), S[3]), S[4]), S[5]), term);
+}
+
+// energy at t1grid.back() (time_steps.cu:641-674 with the CPU sum order)
+__global__ void k_energy_exact(const DevCtx c, const int nrows, double* out) {
+    const int L = c.L;
+    const DModel Mo = c.M;
+    const double t = c.t1grid[nrows - 1];
+    const double2* q = c.KR + (size_t)(nrows - 1) * L;
+    double A = 0.0;
+    for (int j = 0; j < L; ++j) A = add(A, mul(mul(mul(t, c.integ[j]), Df_x(Mo, q[j].x)), q[j].y));
+    out[0] = -add(A, dvd(Df_x(Mo, q[0].x), Mo.T0));
+}
+
+// ConvA / ConvR on device arrays (convolution.cpp:5-50)
+__global__ void k_conv_exact(const DevCtx c, const int kind, const double* f, const double* g,
+                             const int depth, const double t, double* out) {
+    const int L = c.L;
+    if (depth == 1) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            double temp = 0.0;
+            for (int j = 0; j < L; ++j) temp = add(temp, mul(mul(mul(t, c.integ[j]), f[j]), g[j]));
+            out[0] = temp;
+        }
+        return;
+    }
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < depth; r += gridDim.x * blockDim.x) {
+        const double o = conv_row_exact(c, f, g, r);
+        out[r] = mul(o, kind == 0 ? mul(t, c.theta[r]) : mul(t, sub(1.0, c.theta[r])));
+    }
+}
+
+__global__ void k_search(const int mode, const double* list, const int nlist, const double* elem,
+                         const size_t nelem, double* out) {
+    const double last = list[nlist - 1];
+    const ListView lv{list, nlist, last};
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nelem; k += (size_t)gridDim.x * blockDim.x)
+        out[k] = search_pos(mode, lv, __dmul_rn(elem[k], last));
+}
+
+// sparsify indicator per node, one thread per node, reference summation order
+__global__ void k_sparsify_flags(const DevCtx c, const int n, const int variant, const double thr,
+                                 unsigned char* flags) {
+    const int L = c.L;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned char keep;
+        const bool interior = i >= 2 && i + 1 < n;
+        const bool evaluate = interior && (variant != 2 || (i % 2) == 0);
+        if (evaluate) {
+            const double tl = c.t1grid[i - 2], tm = c.t1grid[i];
+            const double td1 = sub(c.t1grid[i - 1], tl), td2 = sub(tm, tl), td3 = sub(c.t1grid[i + 1], tm);
+            const double sc = dvd(td2, 12.0);
+            const double2* X2 = c.KR + (size_t)(i - 2) * L;
+            const double2* X0 = c.KR + (size_t)i * L;
+            const double2* D1 = c.dKR + (size_t)(i - 1) * L;
+            const double2* D3 = c.dKR + (size_t)(i + 1) * L;
+            double val = 0.0;
+            auto term = [&](double f1, double df1, double df2) {
+                return fabs(mul(sc, sub(mul(2.0, f1), mul(td2, add(dvd(df1, td1), dvd(df2, td3))))));
+            };
+            if (variant == 2) {
+                for (int j = 0; j < L; ++j) {
+                    val = add(val, term(sub(X0[j].x, X2[j].x), D1[j].x, D3[j].x));
+                    val = add(val, term(sub(X0[j].y, X2[j].y), D1[j].y, D3[j].y));
+                }
+            } else {
+                for (int j = 0; j < L; ++j) val = add(val, term(sub(X0[j].x, X2[j].x), D1[j].x, D3[j].x));
+                for (int j = 0; j < L; ++j) val = add(val, term(sub(X0[j].y, X2[j].y), D1[j].y, D3[j].y));
+                if (variant == 0)
+                    val = add(val, term(sub(c.rvec[i], c.rvec[i - 2]), c.drvec[i - 1], c.drvec[i + 1]));
+            }
+            keep = (unsigned char)(1 | (val < thr ? 2 : 0) | (val >= thr ? 4 : 0));
+        } else {
+            keep = 0;
+        }
+        flags[i] = keep;  // bit0 evaluated, bit1 val < thr, bit2 val >= thr
+    }
+}
+
+__global__ void k_compact(const DevCtx c, const int* inds, const int* indsD, const double* tfac, const int k,
+                          double2* KRn, double2* dKRn, double* rn, double* drn) {
+    const int L = c.L;
+    const size_t total = (size_t)k * L;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(e / L), j = (int)(e % L);
+        KRn[e] = c.KR[(size_t)inds[r] * L + j];
+        const double f = tfac ? tfac[r] : 1.0;
+        const double2 d = c.dKR[(size_t)indsD[r] * L + j];
+        dKRn[e] = make_double2(mul(f, d.x), mul(f, d.y));
+        if (j == 0) {
+            rn[r] = c.rvec[inds[r]];
+            drn[r] = mul(f, c.drvec[indsD[r]]);
+        }
+    }
+}
+
+__global__ void k_pack(const double* QK, const double* QR, double2* out, size_t count) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        out[e] = make_double2(QK[e], QR[e]);
+}
+__global__ void k_unpack(const double2* in, double* QK, double* QR, size_t count) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = in[e];
+        QK[e] = v.x;
+        QR[e] = v.y;
+    }
+}
+
+// FP64 throughput probe: 8 independent FMA chains per thread.
+__global__ void k_fp64_probe(double* out, int iters) {
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+    const double b = 0.999999, c = 1e-7;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+// ------------------------------------------------------------------------
+// launch wrappers
+template <int M, int K, int P, int P2>
+static cudaError_t launch_main_t(const DevCtx& c, int s, cudaStream_t st) {
+    dim3 grid(c.nch, c.L), block(c.tpb);
+    const size_t smem = (size_t)c.L * sizeof(double2);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_main<M, K, P, P2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        attr_set = true;
+    }
+    k_main<M, K, P, P2><<<grid, block, smem, st>>>(c, s);
+    return cudaGetLastError();
+}
+
+template <int M, int P, int P2>
+static cudaError_t launch_main_k(const DevCtx& c, int s, cudaStream_t st) {
+    switch (c.kpt) {
+        case 1: return launch_main_t<M, 1, P, P2>(c, s, st);
+        case 2: return launch_main_t<M, 2, P, P2>(c, s, st);
+        default: return launch_main_t<M, 4, P, P2>(c, s, st);
+    }
+}
+
+template <int P, int P2>
+static cudaError_t launch_stage_pp(const DevCtx& c, int s, cudaStream_t st) {
+    cudaError_t e = c.m == 10 ? launch_main_k<10, P, P2>(c, s, st) : launch_main_k<0, P, P2>(c, s, st);
+    if (e != cudaSuccess) return e;
+    const int G = (c.L + EPI_T - 1) / EPI_T;
+    k_epi<P, P2><<<G, EPI_T, 0, st>>>(c, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage(const DevCtx& c, int s, cudaStream_t st) {
+    if (c.M.p == 3 && c.M.p2 == 4) return launch_stage_pp<3, 4>(c, s, st);
+    if (c.M.p == 3 && c.M.p2 == 0) return launch_stage_pp<3, 0>(c, s, st);
+    return launch_stage_pp<-1, -1>(c, s, st);
+}
+
+template <int P, int P2>
+static cudaError_t launch_main_pp(const DevCtx& c, int s, cudaStream_t st) {
+    return c.m == 10 ? launch_main_k<10, P, P2>(c, s, st) : launch_main_k<0, P, P2>(c, s, st);
+}
+
+cudaError_t launch_main_only(const DevCtx& c, int s, cudaStream_t st) {
+    if (c.M.p == 3 && c.M.p2 == 4) return launch_main_pp<3, 4>(c, s, st);
+    if (c.M.p == 3 && c.M.p2 == 0) return launch_main_pp<3, 0>(c, s, st);
+    return launch_main_pp<-1, -1>(c, s, st);
+}
+
+cudaError_t launch_epi_only(const DevCtx& c, int s, cudaStream_t st) {
+    const int G = (c.L + EPI_T - 1) / EPI_T;
+    if (c.M.p == 3 && c.M.p2 == 4) k_epi<3, 4><<<G, EPI_T, 0, st>>>(c, s);
+    else if (c.M.p == 3 && c.M.p2 == 0) k_epi<3, 0><<<G, EPI_T, 0, st>>>(c, s);
+    else k_epi<-1, -1><<<G, EPI_T, 0, st>>>(c, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pos_init(const DevCtx& c, int nrows, cudaStream_t st) {
+    k_pos_init<<<1, 256, 0, st>>>(c, nrows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interp_exact(const DevCtx& c, int nrows, const double* p1, const double* p2, cudaStream_t st) {
+    k_pos_b1_exact<<<1, 256, 0, st>>>(c, nrows, p1, p2);
+    const size_t L2 = (size_t)c.L * c.L;
+    const int blocks = (int)((L2 + 255) / 256 < 4096 ? (L2 + 255) / 256 : 4096);
+    k_interp_exact<<<blocks, 256, 0, st>>>(c, nrows, p2);
+    k_rint_exact<<<(c.L + 127) / 128, 128, 0, st>>>(c, nrows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_qkr_exact(const DevCtx& c, int nrows, double2* out, cudaStream_t st) {
+    k_qkr_exact<<<(c.L + 31) / 32, 32, 0, st>>>(c, nrows, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rstep_exact(const DevCtx& c, int nrows, double* out, cudaStream_t st) {
+    k_rstep_exact<<<1, 1, 0, st>>>(c, nrows, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_drstep2_exact(const DevCtx& c, const double* qK, const double* qR, const double* dqK,
+                                 const double* dqR, double t, double* out, cudaStream_t st) {
+    k_drstep2_exact<<<1, 1, 0, st>>>(c, qK, qR, dqK, dqR, t, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_energy_exact(const DevCtx& c, int nrows, double* out, cudaStream_t st) {
+    k_energy_exact<<<1, 1, 0, st>>>(c, nrows, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_conv_exact(const DevCtx& c, int kind, const double* f, const double* g, size_t n, double t,
+                              double* out, cudaStream_t st) {
+    const int depth = (int)(n / c.L);
+    k_conv_exact<<<(depth + 31) / 32, 32, 0, st>>>(c, kind, f, g, depth, t, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_search(const DevCtx& c, const double* list, size_t nlist, const double* elem, size_t nelem,
+                          double* out, cudaStream_t st) {
+    const int blocks = (int)((nelem + 255) / 256 < 4096 ? (nelem + 255) / 256 : 4096);
+    k_search<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(c.search, list, (int)nlist, elem, nelem, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sparsify_flags(const DevCtx& c, int n, int variant, double thr, unsigned char* flags,
+                                  cudaStream_t st) {
+    k_sparsify_flags<<<(n + 63) / 64, 64, 0, st>>>(c, n, variant, thr, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const DevCtx& c, const int* inds, const int* indsD, const double* tfac, int k,
+                           double2* KRn, double2* dKRn, double* rn, double* drn, cudaStream_t st) {
+    const size_t total = (size_t)k * c.L;
+    const int blocks = (int)((total + 255) / 256 < 8192 ? (total + 255) / 256 : 8192);
+    k_compact<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(c, inds, indsD, tfac, k, KRn, dKRn, rn, drn);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_rows(const double* QK, const double* QR, double2* out, size_t count, cudaStream_t st) {
+    const int blocks = (int)((count + 255) / 256 < 8192 ? (count + 255) / 256 : 8192);
+    k_pack<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(QK, QR, out, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st) {
+    k_fp64_probe<<<blocks, threads, 0, st>>>(out, iters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_rows(const double2* in, double* QK, double* QR, size_t count, cudaStream_t st) {
+    const int blocks = (int)((count + 255) / 256 < 8192 ? (count + 255) / 256 : 8192);
+    k_unpack<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, QK, QR, count);
+    return cudaGetLastError();
+}
+
+}  // namespace dyn

@@ -1,0 +1,112 @@
+// Kernel-side structures shared by dyn_kernels.cu and dyn_api.cu.
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+#include "dyn_common.cuh"
+
+namespace dyn {
+
+constexpr int SMAX = 32;      // most stages of one step (SERK2 with q <= 16)
+constexpr int NSAVE = 3;      // SSPRK(10,4) keeps positions of stages 2..4
+constexpr int EPI_T = 32;     // rows per epilogue CTA
+constexpr int EP_N = 16;      // per-CTA epilogue partials
+
+enum StageKind { KIND_TABLEAU = 0, KIND_SERK = 1, KIND_RHS = 2 };
+
+// One RK stage as the device sees it; the host fills an array of these per
+// step (pinned buffer -> one H2D copy), so a captured graph replays any step.
+struct StageDev {
+    int s, kind, last, nrows, n0, nrows_next;
+    int b2_save, b2_reuse;   // main(s): posB2x save/reuse slot, -1 none
+    int pos_save, pos_reuse; // epilogue(s): next stage's posB1x save/reuse slot
+    int nb2_reuse, nb2_save; // next stage's posB2x flags (for the B2 clamp)
+    int ncoef, serk_mode;    // serk_mode: 0 first stage, 1 even, 2 odd
+    int pad0, pad1;
+    double T;        // t1grid.back() while this stage's RHS is evaluated
+    double T_next;   // time of the row this stage writes
+    double tdiff;    // T_next - t1grid[n0-1]
+    double dtr_new;  // delta_t_ratio of the written row
+    double serk_c, serk_c2, serk_b0, serk_bnext;
+    double coef[SMAX];    // tableau: g = g0 + sum_j h_j coef[j]
+    double coef_e[SMAX];  // embedded solution coefficients (last stage)
+};
+
+struct Slots {
+    double q0;            // C(t, theta=0) of the current last row
+    double dr;            // drstep2 of the current step
+    int maxceil;          // B1 Floor clamp of the current stage
+    int maxX;             // B2 clamp of the current stage
+    int saved_maxX[NSAVE];
+    unsigned int counter; // last-block election in the epilogue
+    int pad;
+    // step result, written by the last epilogue block of the last stage
+    double res_err, res_energy, res_r, res_qk0, res_dr;
+};
+
+struct DevCtx {
+    int L, m, nch, search, kpt, tpb;
+    DModel M;
+    const double* theta;
+    const double* phi2;
+    const double* integ;
+    const int* iA1;
+    const int* iA2;
+    const int* iB2;
+    const double* wA1;
+    const double* wA2;
+    const double* wB2;
+    double2* KR;
+    double2* dKR;
+    double* t1grid;
+    double* dtr;
+    double* inv_dtr;
+    double* rvec;
+    double* drvec;
+    double* posB1x;        // [L]
+    double* posB1x_saved;  // [NSAVE][L]
+    double* posB2x;        // [L*L]
+    double* posB2x_saved;  // [NSAVE][L*L]
+    double2* h;            // [SMAX][L]
+    double2* gS;           // SERK running stage value [L]
+    double2* geS;          // SERK previous odd value [L]
+    double2* gfS;          // SERK combination [L]
+    double* part;          // [L][nch][8]
+    double2* rowval;       // [L] (QK^{B1}[i,0], rInt_i)
+    double* epart;         // [G][EP_N]
+    Slots* slots;
+    StageDev* stages;      // [SMAX]
+    double2* rhs_out;      // [L]
+    // materialized interpolation (dyn_interpolate)
+    double* ip;            // [16][L*L]
+    double* rint;          // [L]
+};
+
+// launch wrappers (dyn_kernels.cu)
+cudaError_t launch_stage(const DevCtx& c, int s, cudaStream_t st);
+cudaError_t launch_main_only(const DevCtx& c, int s, cudaStream_t st);
+cudaError_t launch_epi_only(const DevCtx& c, int s, cudaStream_t st);
+cudaError_t launch_pos_init(const DevCtx& c, int nrows, cudaStream_t st);
+cudaError_t launch_interp_exact(const DevCtx& c, int nrows, const double* pos1_given,
+                                const double* pos2_given, cudaStream_t st);
+cudaError_t launch_qkr_exact(const DevCtx& c, int nrows, double2* out, cudaStream_t st);
+cudaError_t launch_rstep_exact(const DevCtx& c, int nrows, double* out, cudaStream_t st);
+cudaError_t launch_drstep2_exact(const DevCtx& c, const double* qK, const double* qR,
+                                 const double* dqK, const double* dqR, double t, double* out,
+                                 cudaStream_t st);
+cudaError_t launch_energy_exact(const DevCtx& c, int nrows, double* out, cudaStream_t st);
+cudaError_t launch_conv_exact(const DevCtx& c, int kind, const double* f, const double* g,
+                              size_t n, double t, double* out, cudaStream_t st);
+cudaError_t launch_search(const DevCtx& c, const double* list, size_t nlist, const double* elem,
+                          size_t nelem, double* out, cudaStream_t st);
+cudaError_t launch_sparsify_flags(const DevCtx& c, int nrows, int variant, double threshold,
+                                  unsigned char* flags, cudaStream_t st);
+cudaError_t launch_compact(const DevCtx& c, const int* inds, const int* indsD, const double* tfac,
+                           int k, double2* KRn, double2* dKRn, double* rn, double* drn,
+                           cudaStream_t st);
+cudaError_t launch_pack_rows(const double* QK, const double* QR, double2* out, size_t count,
+                             cudaStream_t st);
+cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
+cudaError_t launch_unpack_rows(const double2* in, double* QK, double* QR, size_t count,
+                               cudaStream_t st);
+
+}  // namespace dyn

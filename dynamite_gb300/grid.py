@@ -1,0 +1,96 @@
+"""Stencil/quadrature tables: generation (native) and the RG-Evo text format.
+
+`generate` is the reference's `RG-Evo grid` (grid_cli.cpp:35-258, poly
+method) done by the native generator in the library; `load`/`save` read and
+write `Grid_data/<L>/` as the reference does (io_input.cpp:90-110,
+grid_io.cpp:26-263), so tables interchange with RG-Evo in both directions.
+"""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+
+
+@dataclass
+class Grid:
+    L: int
+    theta: np.ndarray
+    phi1: np.ndarray
+    phi2: np.ndarray
+    integ: np.ndarray
+    indsA1: np.ndarray
+    wA1: np.ndarray
+    indsA2: np.ndarray
+    wA2: np.ndarray
+    indsB2: np.ndarray
+    wB2: np.ndarray
+
+    @property
+    def depth(self) -> int:
+        return self.wA1.size // (self.L * self.L)
+
+
+_CACHE: dict = {}
+
+
+def generate(L: int, Tmax: float = 1e5, spline_order: int = 5, interp_order: int = 9,
+             alpha: float = 0.0, delta: float = 0.0, cache: bool = True) -> Grid:
+    key = (L, Tmax, spline_order, interp_order, alpha, delta)
+    if cache and key in _CACHE:
+        return _CACHE[key]
+    m = interp_order + 1
+    L2 = L * L
+    th, it = np.empty(L), np.empty(L)
+    p1, p2 = np.empty(L2), np.empty(L2)
+    i1, i2, i3 = (np.empty(L2, dtype=np.int64) for _ in range(3))
+    w1, w2, w3 = (np.empty(L2 * m) for _ in range(3))
+    i64 = lambda a: a.ctypes.data_as(_lib.i64p)
+    st = _lib.lib().dyn_grid_generate(L, Tmax, spline_order, interp_order, alpha, delta, _lib.ptr(th), _lib.ptr(p1),
+                                      _lib.ptr(p2), _lib.ptr(it), i64(i1), _lib.ptr(w1), i64(i2), _lib.ptr(w2),
+                                      i64(i3), _lib.ptr(w3))
+    _lib.check(st, "dyn_grid_generate")
+    g = Grid(L, th, p1, p2, it, i1, w1, i2, w2, i3, w3)
+    if cache:
+        _CACHE[key] = g
+    return g
+
+
+def _read(path: str, dtype=np.float64) -> np.ndarray:
+    with open(path, "r") as fh:
+        return np.array(fh.read().split(), dtype=dtype)
+
+
+def load(directory: str) -> Grid:
+    """Read Grid_data/<L>/ as written by `RG-Evo grid`."""
+    th = _read(os.path.join(directory, "theta.dat"))
+    L = th.size
+    p1_path = os.path.join(directory, "phi1.dat")
+    p1 = _read(p1_path) if os.path.exists(p1_path) else np.zeros(L * L)
+    return Grid(L, th, p1, _read(os.path.join(directory, "phi2.dat")), _read(os.path.join(directory, "int.dat")),
+                _read(os.path.join(directory, "indsA1y.dat"), np.int64), _read(os.path.join(directory, "weightsA1y.dat")),
+                _read(os.path.join(directory, "indsA2y.dat"), np.int64), _read(os.path.join(directory, "weightsA2y.dat")),
+                _read(os.path.join(directory, "indsB2y.dat"), np.int64), _read(os.path.join(directory, "weightsB2y.dat")))
+
+
+def save(g: Grid, directory: str) -> None:
+    """Write the tables in RG-Evo's layout (17 digits after the point)."""
+    os.makedirs(directory, exist_ok=True)
+    L = g.L
+
+    def vec(name, a):
+        np.savetxt(os.path.join(directory, name), a, fmt="%.17e")
+
+    def mat(name, a, fmt="%.17e"):
+        np.savetxt(os.path.join(directory, name), a.reshape(L, L), fmt=fmt, delimiter="\t")
+
+    vec("theta.dat", g.theta)
+    vec("int.dat", g.integ)
+    mat("phi1.dat", g.phi1)
+    mat("phi2.dat", g.phi2)
+    for name, inds, w in (("A1y", g.indsA1, g.wA1), ("A2y", g.indsA2, g.wA2), ("B2y", g.indsB2, g.wB2)):
+        mat(f"inds{name}.dat", inds, fmt="%d")
+        vec(f"weights{name}.dat", w)

@@ -1,0 +1,230 @@
+/*
+ * dyn.h — C ABI of the GB300-native DYNAMITE hot path.
+ *
+ * One context (dyn_ctx) owns everything the reference keeps in the globals
+ * `sim` (SimulationData, include/simulation/simulation_data.hpp:12-55), `rk`
+ * (RKData, include/EOMs/rk_data.hpp:9-25) and the model constants
+ * (`config`, include/core/config.hpp:18-56; `__constant__ d_p/d_p2/d_lambda`,
+ * src/core/device_constants.cu:4-6): the stencil tables, the two-time
+ * history, the interpolation results and the RK scratch, all resident on one
+ * GPU.  Every function returns a dyn_status; no C++ exception crosses the
+ * ABI.  Host buffers are plain pointers owned by the caller; functions whose
+ * name ends in `_dev` take device pointers.
+ *
+ * Thread safety: a context is used from one host thread at a time.
+ */
+#ifndef DYN_H
+#define DYN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DYN_ABI_VERSION 1
+
+typedef enum {
+    DYN_OK = 0,
+    DYN_ERR_INVALID = -1,     /* bad argument or size */
+    DYN_ERR_CUDA = -2,        /* a CUDA call failed; see dyn_last_error() */
+    DYN_ERR_NOMEM = -3,       /* device or host allocation failed */
+    DYN_ERR_STATE = -4,       /* call not valid in the current state */
+    DYN_ERR_UNSUPPORTED = -5, /* option not built into this library */
+    DYN_ERR_TIMEOUT = -6      /* a bounded device-side wait ran out */
+} dyn_status;
+
+/* RK methods: values of rk->init (runge_kutta.cu:607-615). */
+enum {
+    DYN_RK54 = 1,      /* Dormand-Prince 5(4), 7 stages */
+    DYN_SSPRK104 = 2,  /* SSPRK(10,4), 10 stages */
+    DYN_SERK2_BASE = 2 /* method m >= 3 is SERK2 with q = 2*(m-2) */
+};
+
+/* Arithmetic of the O(L^2) gathers and reductions. */
+enum { DYN_FP64 = 0, DYN_MIXED = 1 };
+
+/* Fractional-position search in t1grid. */
+enum {
+    DYN_SEARCH_BINARY = 0,      /* bsearchPosSorted, search_utils.cpp:13-61 */
+    DYN_SEARCH_LOWER_BOUND = 1  /* bsearch_interp_kernel, search_utils.cu:71-112 */
+};
+
+/* sparsifyNscale variants (the reference has three). */
+enum {
+    DYN_SPARSIFY_CPU = 0,       /* CPU-only build, sparsify_utils.cpp:14-97 */
+    DYN_SPARSIFY_CUDA_HOST = 1, /* CUDA build, host path, sparsify_utils.cu:38-113 */
+    DYN_SPARSIFY_GPU = 2        /* CUDA build, device path, sparsify_utils.cu:154-290 */
+};
+
+/* Which materialized interpolation array dyn_get_interp returns. */
+enum {
+    DYN_QKA1 = 0, DYN_QRA1, DYN_QKA2, DYN_QRA2, DYN_QKB1, DYN_QRB1, DYN_QKB2, DYN_QRB2,
+    DYN_SIGMAKA1, DYN_SIGMARA1, DYN_SIGMAKA2, DYN_SIGMARA2,
+    DYN_SIGMAKB1, DYN_SIGMARB1, DYN_SIGMAKB2, DYN_SIGMARB2,
+    DYN_RINT = 16,    /* [len] */
+    DYN_POSB1X = 17,  /* [len] */
+    DYN_POSB2X = 18   /* [len*len] */
+};
+
+/* Model, grid size and run options (config.hpp:18-56). */
+typedef struct {
+    int p, p2;              /* f(q) = lambda q^p + (1-lambda) q^p2 */
+    double lambda;
+    double T0;              /* initial temperature (1e50 = infinite) */
+    double Gamma;           /* bath temperature */
+    size_t len;             /* L */
+    size_t depth;           /* stencil depth m (interp order + 1) */
+    double delta_t_min;
+    double delta_max;
+    int precision;          /* DYN_FP64 | DYN_MIXED */
+    int search;             /* DYN_SEARCH_* */
+    size_t history_capacity;/* rows to preallocate (0: default) */
+    int device;             /* CUDA device ordinal */
+    void* stream;           /* cudaStream_t to run on; NULL: the context creates one */
+    int use_graph;          /* capture each RK step into a CUDA graph */
+} dyn_config;
+
+/* Grid tables as RG-Evo writes them (grid_cli.cpp:163-215, read back by
+ * io_input.cpp:90-110).  Host pointers; copied at dyn_ctx_create. */
+typedef struct {
+    const double* theta;       /* [len], non-decreasing, theta[len-1] == 1 */
+    const double* phi2;        /* [len*len] */
+    const double* integ;       /* [len] (int.dat) */
+    const int64_t* indsA1y;    /* [len*len] stencil starts */
+    const int64_t* indsA2y;
+    const int64_t* indsB2y;
+    const double* weightsA1y;  /* [len*len*depth] */
+    const double* weightsA2y;
+    const double* weightsB2y;
+} dyn_tables;
+
+/* History in the reference's layout (simulation_data.hpp:32-38); host buffers. */
+typedef struct {
+    size_t n;                 /* rows */
+    double* t1grid;           /* [n] */
+    double* delta_t_ratio;    /* [n] */
+    double* QK;               /* [n*len] row-major */
+    double* QR;
+    double* dQK;
+    double* dQR;
+    double* rvec;             /* [n] */
+    double* drvec;            /* [n] */
+} dyn_state;
+
+/* Controller variables (config.hpp:18-56: delta, delta_old, loop, delta_t, rk->init). */
+typedef struct {
+    double delta_t;
+    double delta;
+    double delta_old;
+    int loop;
+    int method;
+} dyn_controller;
+
+/* What one RK step returns to the driver loop. */
+typedef struct {
+    double delta;   /* error estimate (runge_kutta.cpp:241-251) */
+    double t;       /* t1grid.back() after the step */
+    double r;       /* r(t) of the new last row */
+    double energy;  /* -(t sum_j w_j f'(C_j) R_j + f'(C_0)/T0) at t (time_steps.cu:641-674) */
+    double qk0;     /* C(t, 0) */
+    double dr;      /* dr/dt at the step start (drstep2) */
+} dyn_step_result;
+
+/* Driver loop options (simulation_runner.cpp:125-304). */
+typedef struct {
+    int nsteps;               /* controller iterations to run */
+    double tmax;              /* stop when t >= tmax (<= 0: no limit) */
+    const double* dt_schedule;   /* optional: replay these step sizes (frozen schedule) */
+    const int* method_schedule;  /* with dt_schedule: the method of each step */
+    int gpu_rollback;         /* 1: the CUDA build's rollback on delta > 2 delta_max (:280-304) */
+    /* optional per-step outputs, each [nsteps] */
+    double* out_dt;
+    int* out_method;
+    double* out_delta;
+    double* out_t;
+    double* out_energy;
+    double* out_qk0;
+    double* out_r;
+} dyn_run_params;
+
+/* ---------------------------------------------------------------- basics */
+int dyn_abi_version(void);
+const char* dyn_last_error(void);
+
+/* Replaces import() + copyVectorsToGPU + copyParametersToDevice
+ * (io_input.cpp:90-110, gpu_memory_utils.cu:11-146,195-199). */
+dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tables, void** ctx);
+dyn_status dyn_ctx_destroy(void* ctx);
+dyn_status dyn_sync(void* ctx);
+
+/* t=0 state: initialization.cpp:204-222 (+ the first interpolation, :267-274). */
+dyn_status dyn_state_init(void* ctx, double delta_t);
+/* Load / read back the history (loadSimulationState / copyVectorsToCPU). */
+dyn_status dyn_state_upload(void* ctx, const dyn_state* st);
+dyn_status dyn_state_rows(void* ctx, size_t* n);
+dyn_status dyn_state_download(void* ctx, dyn_state* st);
+dyn_status dyn_controller_get(void* ctx, dyn_controller* c);
+dyn_status dyn_controller_set(void* ctx, const dyn_controller* c);
+
+/* ---------------------------------------------------------- the path */
+/* interpolateGPU (interpolation_core.cu:63-159): fills the 16 [len*len]
+ * arrays, rInt and the positions.  posB1x/posB2x: optional host arrays to
+ * use as positions instead of searching (same == 1 in the reference). */
+dyn_status dyn_interpolate(void* ctx, const double* posB1x, const double* posB2x);
+dyn_status dyn_get_interp(void* ctx, int which, double* host_out);
+
+/* QKRstepGPU (time_steps.cu:327-408) on the materialized arrays. */
+dyn_status dyn_qkr_step(void* ctx, double* hK, double* hR);
+/* The same right-hand side computed by the fused stage kernel (no arrays). */
+dyn_status dyn_rhs(void* ctx, double* hK, double* hR);
+/* rstepGPU (time_steps.cu:410-472) of the last row; drstep2GPU (:564-639)
+ * on caller rows; energyGPU (:641-674). */
+dyn_status dyn_rstep(void* ctx, double* r);
+dyn_status dyn_drstep2(void* ctx, const double* qK, const double* qR, const double* dqK,
+                       const double* dqR, double t, double* dr);
+dyn_status dyn_energy(void* ctx, double* e);
+/* ConvAGPU / ConvRGPU (convolution.cu:64-230): kind 0 = A, 1 = R; f, g,
+ * out are device arrays, n = len (1-D) or len*len (2-D). */
+dyn_status dyn_conv_dev(void* ctx, int kind, const double* f, const double* g, size_t n, double t,
+                        double* out);
+/* bsearchPosSortedGPU (search_utils.cu:273-319): out[k] = position of
+ * elem[k] * list[nlist-1] in list, device arrays. */
+dyn_status dyn_search_dev(void* ctx, const double* list, size_t nlist, const double* elem,
+                          size_t nelem, double* out);
+
+/* One RK step: updateGPU / update (runge_kutta.cu:607-615, runge_kutta.cpp:254-261). */
+dyn_status dyn_update(void* ctx, int method, double delta_t, dyn_step_result* res);
+/* The driver loop (simulation_runner.cpp:125-304) for p->nsteps iterations. */
+dyn_status dyn_run(void* ctx, const dyn_run_params* p, dyn_step_result* last);
+/* sparsifyNscale[GPU] (sparsify_utils.*): returns the new row count. */
+dyn_status dyn_sparsify(void* ctx, double threshold, int variant, size_t* n_out);
+/* rollbackState (simulation_control.cpp:14-123). */
+dyn_status dyn_rollback(void* ctx, int nrows);
+
+/* The last history row C(t, theta_j t), R(t, theta_j t) into host buffers
+ * (what the driver loop reads after each step, simulation_runner.cpp:306-310). */
+dyn_status dyn_last_row(void* ctx, double* qK, double* qR);
+
+/* ----------------------------------------------------------- measurement */
+/* Average device time of the two stage kernels for the current state, timed
+ * with CUDA events on the context's stream over `reps` launches. */
+dyn_status dyn_profile_stage(void* ctx, int reps, float* ms_main, float* ms_epilogue);
+/* Measured FP64 FMA throughput of the current device (GFLOP/s, 2 flop/FMA). */
+dyn_status dyn_probe_fp64(int device, double* gflops);
+
+/* ------------------------------------------------------------ tables */
+/* `RG-Evo grid -L len -M Tmax -s spline_order -m poly -o interp_order
+ * -a alpha -D delta` (grid_cli.cpp:35-258) without the files: fills the
+ * tables the solver reads (caller-allocated; phi1 may be NULL; depth =
+ * interp_order + 1).  Host only, no GPU needed. */
+dyn_status dyn_grid_generate(size_t len, double Tmax, int spline_order, int interp_order, double alpha,
+                             double delta, double* theta, double* phi1, double* phi2, double* integ,
+                             int64_t* indsA1y, double* weightsA1y, int64_t* indsA2y, double* weightsA2y,
+                             int64_t* indsB2y, double* weightsB2y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DYN_H */

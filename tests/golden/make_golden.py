@@ -1,0 +1,135 @@
+"""Generate the golden vectors in tests/golden/ by running the reference itself.
+
+The reference DYNAMITE CPU implementation is compiled from its own sources by
+oracle/Makefile (oracle/_ref/libdynref.so, IEEE build, single thread) and driven
+through the harness in oracle/ref_harness.cpp.  The vectors pin both the C
+restatement (oracle/dyn_oracle.c) and the CUDA path.
+
+    python tests/golden/make_golden.py        # needs the reference sources
+
+Cases (one .npz per grid size):
+  grid       tables from the reference generator (poly-9, spline order 5)
+  t0_*       t=0 state and its first interpolation / right-hand side
+  mid_*      state after an adaptive RK54 run (40 controller iterations),
+             interpolation at fresh (binary-search) positions, QKstep/QRstep,
+             rstep, drstep2, energy
+  rk54_*     one RK54 step from the mid state
+  ssp_*      one SSPRK(10,4) step from the mid state
+  traj_*     the reference controller run from t=0: per-step dt, method,
+             error, time, energy, and the final history
+  spars_*    sparsifyNscale (CPU-only build variant) of the trajectory state
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+CASES = [
+    # L, Tmax, model, trajectory steps
+    (32, 10.0, O.Model(p=3, p2=4, lam=0.5, T0=1e50, Gamma=0.6), 120),
+    (64, 100.0, O.Model(p=3, p2=0, lam=0.5, T0=1e50, Gamma=0.8), 80),
+]
+
+
+def state_dict(prefix: str, st: O.State) -> dict:
+    return {f"{prefix}_{k}": getattr(st, k) for k in
+            ("t1grid", "dtr", "QK", "QR", "dQK", "dQR", "rvec", "drvec", "posB1xOld", "posB2xOld")}
+
+
+def make(L: int, Tmax: float, model: O.Model, nsteps: int) -> dict:
+    out = {}
+    g = O.Reference.grid(L, Tmax=Tmax)
+    for k in ("theta", "phi1", "phi2", "integ", "indsA1", "wA1", "indsA2", "wA2", "indsB2", "wB2"):
+        out[f"grid_{k}"] = getattr(g, k)
+    out["model"] = np.array([model.p, model.p2, model.lam, model.T0, model.Gamma, model.delta_t_min,
+                             model.delta_max, Tmax])
+    ref = O.Reference(g, model, threads=1)
+
+    # t = 0
+    ref.init_state()
+    out.update(state_dict("t0", ref.get_state()))
+    for w in range(17):
+        out[f"t0_interp{w}"] = ref.interp(w)
+    out["t0_qk"] = ref.qkstep()
+    out["t0_qr"] = ref.qrstep()
+
+    # trajectory with the reference controller
+    ref.init_state()
+    tr = ref.run(nsteps)
+    for k, v in tr.items():
+        out[f"traj_{k}"] = v
+    out.update(state_dict("traj_final", ref.get_state()))
+
+    # mid state: first 40 iterations of the same run
+    ref.init_state()
+    ref.run(40)
+    mid = ref.get_state()
+    out.update(state_dict("mid", mid))
+    out["mid_ctl"] = np.array([O.Reference.lib().dynref_get_delta_t()], dtype=np.float64)
+    ref.interpolate()  # fresh positions (binary search)
+    for w in range(17):
+        out[f"mid_interp{w}"] = ref.interp(w)
+    out["mid_qk"] = ref.qkstep()
+    out["mid_qr"] = ref.qrstep()
+    out["mid_rstep"] = np.array([ref.rstep()])
+    st = ref.get_state()
+    n = st.n
+    qK, qR = st.QK[(n - 1) * L:], st.QR[(n - 1) * L:]
+    out["mid_drstep2"] = np.array([ref.drstep2(qK, qR, out["mid_qk"], out["mid_qr"], st.t1grid[-1])])
+    out["mid_energy"] = np.array([ref.energy(st.t1grid[-1])])
+
+    dt = float(out["mid_ctl"][0])
+    for tag, method in (("rk54", 1), ("ssp", 2)):
+        ref.set_state(mid)
+        ref.interpolate(mid.posB1xOld, mid.posB2xOld, True)
+        err = ref.update(method, dt)
+        out[f"{tag}_dt"] = np.array([dt])
+        out[f"{tag}_err"] = np.array([err])
+        out.update(state_dict(tag, ref.get_state()))
+
+    # sparsify the trajectory state (CPU-only build variant)
+    final = O.State(*(out[f"traj_final_{k}"] for k in
+                      ("t1grid", "dtr", "QK", "QR", "dQK", "dQR", "rvec", "drvec", "posB1xOld", "posB2xOld")))
+    thr = float(np.quantile(_indicators(final, L), 0.5))
+    ref.set_state(final)
+    ref.sparsify(thr)
+    out["spars_threshold"] = np.array([thr])
+    out.update(state_dict("spars", ref.get_state()))
+    return out
+
+
+def _indicators(st: O.State, L: int) -> np.ndarray:
+    """Node error indicators (sparsify_utils.cpp:19-56), to pick a threshold that drops about half."""
+    t = st.t1grid
+    QK, QR, dQK, dQR = (a.reshape(-1, L) for a in (st.QK, st.QR, st.dQK, st.dQR))
+    vals = []
+    for i in range(2, t.size - 1):
+        td1, td2, td3 = t[i - 1] - t[i - 2], t[i] - t[i - 2], t[i + 1] - t[i]
+        v = 0.0
+        for X, dX in ((QK, dQK), (QR, dQR)):
+            v += np.abs(td2 / 12.0 * (2 * (X[i] - X[i - 2]) - td2 * (dX[i - 1] / td1 + dX[i + 1] / td3))).sum()
+        vals.append(v)
+    return np.array(vals)
+
+
+def main():
+    if not O.Reference.available():
+        O.build(reference=True)
+    for L, Tmax, model, nsteps in CASES:
+        data = make(L, Tmax, model, nsteps)
+        path = os.path.join(HERE, f"golden_L{L}.npz")
+        np.savez_compressed(path, **data)
+        print(path, os.path.getsize(path))
+
+
+if __name__ == "__main__":
+    main()

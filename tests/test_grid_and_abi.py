@@ -1,0 +1,74 @@
+"""Native grid generator vs the reference generator's tables, the RG-Evo text
+format round trip, and the C-ABI library surface (no GPU)."""
+import ctypes as C
+import os
+import platform
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+
+FIELDS = ("theta", "phi1", "phi2", "integ", "indsA1", "wA1", "indsA2", "wA2", "indsB2", "wB2")
+
+
+@pytest.mark.parametrize("L,Tmax", [(32, 10.0), (64, 100.0)])
+def test_generator_matches_reference_golden(product_built, L, Tmax):
+    g = product_built.grid.generate(L, Tmax=Tmax, cache=False)
+    gold = load_golden(L)
+    exact = platform.machine() in ("x86_64", "AMD64")
+    for f in FIELDS:
+        a, b = getattr(g, f), gold[f"grid_{f}"]
+        if f.startswith("inds") or exact:
+            np.testing.assert_array_equal(a, b, err_msg=f)
+        else:  # 128-bit long double on aarch64: last-bit differences only
+            np.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-13, err_msg=f)
+
+
+def test_generator_invariants(product_built):
+    """theta spans [0,1]; quadrature integrates 1; poly-9 stencils reproduce
+    monomials up to degree 9 (the reference's own invariant,
+    src/grid/test_interpolation_weights.cpp:36-66, tolerance 5e-13)."""
+    g = product_built.grid.generate(128, Tmax=1e5, cache=False)
+    L, m = g.L, g.depth
+    assert g.theta[0] == 0.0 and g.theta[-1] == 1.0 and np.all(np.diff(g.theta) >= 0)
+    assert abs(g.integ.sum() - 1.0) < 1e-12
+    xq = g.phi1
+    w = g.wA1.reshape(L * L, m)
+    idx = g.indsA1[:, None] + np.arange(m)[None, :]
+    for d in range(0, 10):
+        approx = (w * g.theta[idx] ** d).sum(axis=1)
+        assert np.max(np.abs(approx - xq ** d)) < 5e-13, d
+
+
+def test_text_format_round_trip(product_built, tmp_path):
+    g = product_built.grid.generate(32, Tmax=10.0, cache=False)
+    product_built.grid.save(g, str(tmp_path))
+    h = product_built.grid.load(str(tmp_path))
+    for f in FIELDS:
+        np.testing.assert_array_equal(getattr(g, f), getattr(h, f), err_msg=f)
+
+
+def _declared_symbols():
+    with open(os.path.join(ROOT, "include", "dyn.h")) as fh:
+        text = fh.read()
+    return sorted(set(re.findall(r"^\s*(?:dyn_status|int|const char\*)\s+(dyn_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(product_built):
+    lib = C.CDLL(product_built._lib.LIB_PATH)
+    names = _declared_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert lib.dyn_abi_version() == 1
+
+
+def test_invalid_arguments_rejected_without_touching_the_gpu(product_built):
+    L = product_built.lib()
+    h = C.c_void_p()
+    assert L.dyn_ctx_create(None, None, C.byref(h)) == -1
+    assert b"null" in L.dyn_last_error()
+    assert L.dyn_update(None, 1, 1e-3, None) == -1
+    assert L.dyn_sparsify(None, 1e-10, 0, None) == -1

@@ -1,0 +1,154 @@
+"""The CPU oracle pinned against the reference (no GPU).
+
+* the C restatement (oracle/dyn_oracle.c) reproduces the committed golden
+  vectors — made by running the reference itself — bit for bit;
+* where the reference sources are present, the compiled reference
+  (oracle/_ref) and the restatement agree bit for bit on fresh inputs too.
+"""
+import numpy as np
+import pytest
+
+from helpers import STATE_FIELDS, grid_from, model_from, state_from
+
+import oracle as O
+from conftest import load_golden
+
+SIZES = (32, 64)
+
+
+def port_for(g, search_mode=0):
+    return O.Port(grid_from(g, O.Grid), model_from(g, O.Model), search_mode=search_mode, threads=2)
+
+
+def assert_state_equal(st, g, prefix):
+    for k in STATE_FIELDS:
+        np.testing.assert_array_equal(getattr(st, k), g[f"{prefix}_{k}"], err_msg=f"{prefix}_{k}")
+
+
+@pytest.mark.parametrize("L", SIZES)
+def test_t0_state_and_interpolation(oracle_built, L):
+    g = load_golden(L)
+    p = port_for(g)
+    p.init_state()
+    assert_state_equal(p.get_state(), g, "t0")
+    for w in range(17):
+        np.testing.assert_array_equal(p.interp(w), g[f"t0_interp{w}"], err_msg=f"interp {w}")
+    np.testing.assert_array_equal(p.qkstep(), g["t0_qk"])
+    np.testing.assert_array_equal(p.qrstep(), g["t0_qr"])
+
+
+@pytest.mark.parametrize("L", SIZES)
+def test_mid_state_kernels(oracle_built, L):
+    g = load_golden(L)
+    p = port_for(g)
+    st = state_from(g, "mid", O.State)
+    p.set_state(st)
+    p.interpolate()
+    for w in range(17):
+        if w == 10:
+            continue  # SigmaKA2 is never computed by the reference CPU interpolate
+        np.testing.assert_array_equal(p.interp(w), g[f"mid_interp{w}"], err_msg=f"interp {w}")
+    qk, qr = p.qkstep(), p.qrstep()
+    np.testing.assert_array_equal(qk, g["mid_qk"])
+    np.testing.assert_array_equal(qr, g["mid_qr"])
+    assert p.rstep() == g["mid_rstep"][0]
+    L_ = g["grid_theta"].size
+    n = st.n
+    qK, qR = st.QK[(n - 1) * L_:], st.QR[(n - 1) * L_:]
+    assert p.drstep2(qK, qR, qk, qr, st.t1grid[-1]) == g["mid_drstep2"][0]
+    assert p.energy(st.t1grid[-1]) == g["mid_energy"][0]
+
+
+@pytest.mark.parametrize("L", SIZES)
+@pytest.mark.parametrize("tag,method", [("rk54", 1), ("ssp", 2)])
+def test_single_steps(oracle_built, L, tag, method):
+    g = load_golden(L)
+    p = port_for(g)
+    st = state_from(g, "mid", O.State)
+    p.set_state(st)
+    p.interpolate(st.posB1xOld, st.posB2xOld, True)
+    err = p.update(method, float(g[f"{tag}_dt"][0]))
+    assert err == g[f"{tag}_err"][0]
+    assert_state_equal(p.get_state(), g, tag)
+
+
+@pytest.mark.parametrize("L", SIZES)
+def test_trajectory_with_controller(oracle_built, L):
+    g = load_golden(L)
+    p = port_for(g)
+    p.init_state()
+    n = g["traj_dt"].size
+    tr = p.run(n)
+    for k in ("dt", "method", "delta", "t", "energy"):
+        np.testing.assert_array_equal(tr[k], g[f"traj_{k}"], err_msg=k)
+    assert_state_equal(p.get_state(), g, "traj_final")
+
+
+@pytest.mark.parametrize("L", SIZES)
+def test_sparsify_cpu_variant(oracle_built, L):
+    g = load_golden(L)
+    p = port_for(g)
+    p.set_state(state_from(g, "traj_final", O.State))
+    p.sparsify(float(g["spars_threshold"][0]), 0)
+    assert_state_equal(p.get_state(), g, "spars")
+
+
+def test_search_modes_agree_on_values(oracle_built):
+    """Seeded with positions from an earlier time (as in the RK stages), the
+    interpolation search finds the same interval as the binary search; the
+    fractional positions differ only by the rounding of the two formulas."""
+    rng = np.random.default_rng(1)
+    lst = np.concatenate([[0.0], np.cumsum(rng.uniform(0.1, 1.0, 300))])
+    L = 64
+    elem = np.sort(rng.uniform(0, 1, L))
+    elem[-1] = 1.0
+    b = O.Port.bsearch(lst, elem * lst[-1])
+    seeds = O.Port.bsearch(lst, elem * lst[-1] * 0.98)
+    i = O.Port.isearch(L, lst, elem, seeds)
+    assert np.max(np.abs(b - i) / b) < 4e-15
+
+
+@pytest.mark.skipif(not O.Reference.available(), reason="reference sources not built here")
+@pytest.mark.parametrize("L,Tmax", [(48, 20.0), (96, 1000.0)])
+def test_port_equals_compiled_reference(oracle_built, L, Tmax):
+    g = O.Reference.grid(L, Tmax=Tmax)
+    m = O.Model(p=3, p2=4, lam=0.3, Gamma=0.7)
+    # one OpenMP thread: the reference's 1-D ConvA is an OpenMP reduction
+    # whose summation order depends on the (process-wide) thread count
+    port = O.Port(g, m, search_mode=0, threads=1)
+    ref = O.Reference(g, m, threads=1)
+    ref.init_state()
+    port.init_state()
+    r1, r2 = ref.run(50), port.run(50)
+    for k in r1:
+        np.testing.assert_array_equal(r1[k], r2[k], err_msg=k)
+    s1, s2 = ref.get_state(), port.get_state()
+    for k in STATE_FIELDS + ("posB1xOld", "posB2xOld"):
+        np.testing.assert_array_equal(getattr(s1, k), getattr(s2, k), err_msg=k)
+    for w in range(17):
+        np.testing.assert_array_equal(ref.interp(w), port.interp(w), err_msg=f"interp {w}")
+    e1, e2 = ref.update(2, 2e-5), port.update(2, 2e-5)
+    assert e1 == e2
+    thr = 1e-9
+    ref.sparsify(thr)
+    port.sparsify(thr, 0)
+    s1, s2 = ref.get_state(), port.get_state()
+    for k in STATE_FIELDS:
+        np.testing.assert_array_equal(getattr(s1, k), getattr(s2, k), err_msg=k)
+
+
+@pytest.mark.skipif(not O.Reference.available(), reason="reference sources not built here")
+def test_search_functions_equal_reference(oracle_built):
+    rng = np.random.default_rng(7)
+    lst = np.concatenate([[0.0], np.cumsum(rng.uniform(1e-3, 1.0, 500))])
+    elem = np.concatenate([rng.uniform(0, lst[-1], 2000), lst[::7], [0.0, lst[-1]]])
+    np.testing.assert_array_equal(O.Reference.bsearch(lst, elem), O.Port.bsearch(lst, elem))
+
+
+def test_serk_coefficients_consistent(oracle_built):
+    """SERK2(q) Chebyshev coefficients (runge_kutta.cu:228-272): the stability
+    polynomial at z=0 gives the identity, so the weights sum to 1."""
+    for q in (2, 4, 6):
+        b = O.Port.serk_coeffs(q)
+        assert b.size == 2 * q + 1
+        assert abs(b.sum() - 1.0) < 1e-12
