@@ -67,6 +67,20 @@ class RunParams(C.Structure):
     ]
 
 
+class NoAllocRHS(C.Structure):
+    """dyn_noalloc_rhs: every pointer is a device address owned by the caller."""
+
+    _fields_ = [
+        ("p", C.c_int), ("p2", C.c_int), ("lam", C.c_double), ("T0", C.c_double), ("Gamma", C.c_double),
+        ("len", C.c_size_t), ("depth", C.c_size_t), ("rows", C.c_size_t), ("search", C.c_int),
+        ("theta", C.c_void_p), ("phi2", C.c_void_p), ("integ", C.c_void_p),
+        ("indsA1y", C.c_void_p), ("indsA2y", C.c_void_p), ("indsB2y", C.c_void_p),
+        ("weightsA1y", C.c_void_p), ("weightsA2y", C.c_void_p), ("weightsB2y", C.c_void_p),
+        ("KR", C.c_void_p), ("dKR", C.c_void_p), ("t1grid", C.c_void_p), ("delta_t_ratio", C.c_void_p),
+        ("rvec", C.c_void_p), ("drvec", C.c_void_p), ("out", C.c_void_p),
+    ]
+
+
 _lib = None
 
 
@@ -110,6 +124,7 @@ def lib():
             "dyn_last_row": ([vp, dp, dp], C.c_int),
             "dyn_profile_stage": ([vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
             "dyn_probe_fp64": ([C.c_int, dp], C.c_int),
+            "dyn_rhs_noalloc": ([C.POINTER(NoAllocRHS), vp], C.c_int),
             "dyn_grid_generate": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                    dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
         }

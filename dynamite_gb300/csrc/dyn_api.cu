@@ -379,6 +379,10 @@ Ctx* C(void* p) { return static_cast<Ctx*>(p); }
 
 }  // namespace
 
+namespace dyn {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}
+
 extern "C" {
 
 int dyn_abi_version(void) { return DYN_ABI_VERSION; }

@@ -214,6 +214,44 @@ dyn_status dyn_profile_stage(void* ctx, int reps, float* ms_main, float* ms_epil
 /* Measured FP64 FMA throughput of the current device (GFLOP/s, 2 flop/FMA). */
 dyn_status dyn_probe_fp64(int device, double* gflops);
 
+/* ------------------------------------------------- allocation-free RHS */
+/* No counterpart in the reference.  The right-hand side of dyn_rhs for
+ * callers that cannot allocate device memory (a driver working inside a
+ * device pool it does not own, or one that has handed all free memory to its
+ * history): every input and the output are the caller's device buffers, in
+ * this library's layout; the kernels' scratch is a fixed file-scope device
+ * array (about 0.5 MB per GPU, held from library load to process exit).
+ * The first call on each device resolves that array's address (make it
+ * before any stream capture); calls that overlap on the GPU race on it.
+ * Limits: len <= DYN_NOALLOC_MAX_LEN, rows <= DYN_NOALLOC_MAX_ROWS;
+ * larger sizes are rejected with DYN_ERR_INVALID.  Enqueued on `stream`
+ * (cudaStream_t, NULL = default stream); the caller synchronizes. */
+#define DYN_NOALLOC_MAX_LEN 1024
+#define DYN_NOALLOC_MAX_ROWS 16384
+typedef struct {
+    int p, p2;
+    double lambda, T0, Gamma;
+    size_t len, depth, rows;
+    int search;                         /* DYN_SEARCH_* */
+    const double* theta;                /* [len] */
+    const double* phi2;                 /* [len*len] */
+    const double* integ;                /* [len] */
+    const int32_t* indsA1y;             /* [len*len] stencil starts */
+    const int32_t* indsA2y;
+    const int32_t* indsB2y;
+    const double* weightsA1y;           /* [len*len*depth] */
+    const double* weightsA2y;
+    const double* weightsB2y;
+    const double* KR;                   /* [rows*len][2]: (QK, QR) pairs, row-major */
+    const double* dKR;                  /* [rows*len][2]: (dQK, dQR) pairs */
+    const double* t1grid;               /* [rows] */
+    const double* delta_t_ratio;        /* [rows] */
+    const double* rvec;                 /* [rows] */
+    const double* drvec;                /* [rows] */
+    double* out;                        /* [len][2]: (hK, hR) pairs */
+} dyn_noalloc_rhs;
+dyn_status dyn_rhs_noalloc(const dyn_noalloc_rhs* args, void* stream);
+
 /* ------------------------------------------------------------ tables */
 /* `RG-Evo grid -L len -M Tmax -s spline_order -m poly -o interp_order
  * -a alpha -D delta` (grid_cli.cpp:35-258) without the files: fills the
