@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--L", type=int, default=512)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-mixed", dest="mixed", action="store_false", help="skip the mixed-precision measurement")
     return ap.parse_args()
 
 
@@ -283,6 +284,32 @@ def run_ours(args):
         t_e2e = float(tt[0])
     e2e_value = world * e2e_steps / t_e2e
 
+    # ---- the mixed-precision form on the same state (FP32 gathers/convolutions)
+    mixed = None
+    if args.mixed:
+        st0 = sim.download()
+        c0 = sim.controller
+        msim = D.Simulation(grid, D.Model(**model_kw()), precision="mixed", device=dev, use_graph=True,
+                            history_capacity=cap, stream=stream.cuda_stream)
+        msim.upload(st0)
+        msim.set_controller(c0["delta_t"], c0["method"], c0["delta"], c0["delta_old"], c0["loop"])
+        msim.run(args.warmup)
+        mev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            mev[k][0].record(stream)
+            msim.run(1)
+            mev[k][1].record(stream)
+        torch.cuda.synchronize()
+        t_mix = sum(a.elapsed_time(b) for a, b in mev) / 1e3
+        mm, me = msim.profile_stage(reps=20)
+        mixed = {"value": args.steps / t_mix, "unit": UNIT, "ms_per_step": 1e3 * t_mix / args.steps,
+                 "stage_ms": {"main": mm, "epilogue": me},
+                 "speedup_vs_fp64": (args.steps / t_mix) / (args.steps / (dev_ms / 1e3))}
+        msim.close()
+
     if rank != 0:
         return
     # ---- roofline of the dominant kernel (gather + convolution), timed live
@@ -321,6 +348,7 @@ def run_ours(args):
         "stage_ms": {"main": ms_main, "epilogue": ms_epi},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "mixed": mixed,
     }
     print(json.dumps(line))
 

@@ -161,9 +161,9 @@ struct Ctx {
         drop_graphs();
         void* bufs[] = {(void*)d.theta, (void*)d.phi2, (void*)d.integ, (void*)d.iA1, (void*)d.iA2, (void*)d.iB2,
                         (void*)d.wA1, (void*)d.wA2, (void*)d.wB2, d.KR, d.dKR, d.t1grid, d.dtr, d.inv_dtr,
-                        d.rvec, d.drvec, d.posB1x, d.posB1x_saved, d.posB2x, d.posB2x_saved, d.h, d.gS,
+                        d.rvec, d.drvec, d.posB1x, d.posB1x_next, d.posB1x_saved, d.posB2x, d.posB2x_saved, d.h, d.gS,
                         d.geS, d.gfS, d.part, d.rowval, d.epart, d.slots, d.stages, d.rhs_out, d.ip,
-                        d.rint, scratch_dev};
+                        d.rint, scratch_dev, (void*)d.wA1f, (void*)d.wA2f, (void*)d.wB2f, d.KRf, d.dKRf};
         for (void* b : bufs) if (b) cudaFree(b);
         std::memset(&d, 0, sizeof d);
         scratch_dev = nullptr;
@@ -193,6 +193,14 @@ struct Ctx {
         if ((s = dalloc(&KR, ncap * L)) || (s = dalloc(&dKR, ncap * L)) || (s = dalloc(&t1g, ncap)) ||
             (s = dalloc(&dt, ncap)) || (s = dalloc(&idt, ncap)) || (s = dalloc(&rv, ncap)) || (s = dalloc(&drv, ncap)))
             return s;
+        float2 *KRf = nullptr, *dKRf = nullptr;
+        // +16 elements: the 16-byte segment loads of the mixed kernel may touch
+        // one element past the end of the last row
+        if (d.mixed && ((s = dalloc(&KRf, ncap * L + 16)) || (s = dalloc(&dKRf, ncap * L + 16)))) return s;
+        if (n && d.mixed) {
+            CK(cudaMemcpyAsync(KRf, d.KRf, n * L * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(dKRf, d.dKRf, n * L * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+        }
         if (n) {
             CK(cudaMemcpyAsync(KR, d.KR, n * L * sizeof(double2), cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(dKR, d.dKR, n * L * sizeof(double2), cudaMemcpyDeviceToDevice, st));
@@ -207,6 +215,12 @@ struct Ctx {
                         (void*)d.drvec})
             if (b) cudaFree(b);
         d.KR = KR; d.dKR = dKR; d.t1grid = t1g; d.dtr = dt; d.inv_dtr = idt; d.rvec = rv; d.drvec = drv;
+        if (d.mixed) {
+            if (d.KRf) cudaFree(d.KRf);
+            if (d.dKRf) cudaFree(d.dKRf);
+            d.KRf = KRf;
+            d.dKRf = dKRf;
+        }
         cap = ncap;
         drop_graphs();
         return DYN_OK;
@@ -222,9 +236,26 @@ struct Ctx {
         return DYN_OK;
     }
 
+    // FP32 mirror of rows [0, n) from the FP64 master (mixed form)
+    dyn_status mirror_all() {
+        if (!d.mixed || n == 0) return DYN_OK;
+        CK(launch_mirror_rows(d.KR, d.KRf, n * L, st));
+        CK(launch_mirror_rows(d.dKR, d.dKRf, n * L, st));
+        return DYN_OK;
+    }
+
     dyn_status pos_init() {
         CK(launch_pos_init(d, (int)n, st));
         return DYN_OK;
+    }
+
+    // With theta[L-1] == phi2[L*L-1] == 1 (checked at creation) the largest
+    // position of both searches is the last row exactly, so the reference's
+    // clamps ceil(max posB1x) - 1 (interpolation_core.cpp:58-67) and
+    // (size_t)(posB2x[L*L-1] - 0.5) (index_mat.cpp:189) are nrows - 1.
+    static void set_clamps(StageDev& sp) {
+        sp.maxceil = sp.nrows - 1 < 1 ? 1 : sp.nrows - 1;
+        sp.maxX = sp.nrows - 1;
     }
 
     int stages_of(int method) const {
@@ -314,6 +345,7 @@ struct Ctx {
             sp.last = s == S - 1;
             sp.n0 = (int)n0;
             sp.nrows = s == 0 ? (int)n0 : (int)n0 + 1;
+            set_clamps(sp);
             sp.nrows_next = (int)n0 + 1;
             sp.T = s == 0 ? T0 : Tn[s - 1];
             sp.T_next = Tn[s];
@@ -393,7 +425,7 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     *out = nullptr;
     const size_t L = cfg->len, m = cfg->depth;
     if (L < 4 || L > 4096 || m < 2 || m > L) return fail(DYN_ERR_INVALID, "len must be in [4, 4096] and 2 <= depth <= len");
-    if (cfg->precision != DYN_FP64) return fail(DYN_ERR_UNSUPPORTED, "precision not available in this context type");
+    if (cfg->precision != DYN_FP64 && cfg->precision != DYN_MIXED) return fail(DYN_ERR_INVALID, "unknown precision");
     if (!tb->theta || !tb->phi2 || !tb->integ || !tb->indsA1y || !tb->indsA2y || !tb->indsB2y || !tb->weightsA1y ||
         !tb->weightsA2y || !tb->weightsB2y)
         return fail(DYN_ERR_INVALID, "missing table");
@@ -433,9 +465,12 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     d.L = (int)L;
     d.m = (int)m;
     d.search = cfg->search;
-    // tile shape: targets per thread x threads per CTA (see dyn_autotune)
-    d.tpb = 64;
-    d.kpt = L >= 512 ? 4 : (L >= 256 ? 2 : 1);
+    d.mixed = cfg->precision == DYN_MIXED;
+    // tile shape: threads per CTA x targets per thread.  FP64: few wide CTAs
+    // amortize the FP64 reduction; mixed: one target per thread keeps more
+    // warps in flight for the latency-bound gathers.
+    d.tpb = d.mixed ? 128 : 64;
+    d.kpt = d.mixed ? 1 : (L >= 512 ? 4 : (L >= 256 ? 2 : 1));
     d.nch = (int)((L + (size_t)d.tpb * d.kpt - 1) / ((size_t)d.tpb * d.kpt));
     DModel& M = d.M;
     M.p = cfg->p;
@@ -455,7 +490,7 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     int *a1, *a2, *b2;
     if ((s = dalloc(&th, L)) || (s = dalloc(&p2, L2)) || (s = dalloc(&it, L)) || (s = dalloc(&a1, L2)) ||
         (s = dalloc(&a2, L2)) || (s = dalloc(&b2, L2)) || (s = dalloc(&w1, L2 * m)) || (s = dalloc(&w2, L2 * m)) ||
-        (s = dalloc(&w3, L2 * m)) || (s = dalloc(&d.posB1x, L)) || (s = dalloc(&d.posB1x_saved, NSAVE * L)) ||
+        (s = dalloc(&w3, L2 * m)) || (s = dalloc(&d.posB1x, L)) || (s = dalloc(&d.posB1x_next, L)) || (s = dalloc(&d.posB1x_saved, NSAVE * L)) ||
         (s = dalloc(&d.posB2x, L2)) || (s = dalloc(&d.posB2x_saved, NSAVE * L2)) ||
         (s = dalloc(&d.h, (size_t)SMAX * L)) || (s = dalloc(&d.gS, L)) || (s = dalloc(&d.geS, L)) ||
         (s = dalloc(&d.gfS, L)) || (s = dalloc(&d.part, L * (size_t)d.nch * 8)) || (s = dalloc(&d.rowval, L)) ||
@@ -479,6 +514,16 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     UP(w3, tb->weightsB2y, L2 * m * sizeof(double));
 #undef UP
     cudaMemset(d.slots, 0, sizeof(Slots));
+    if (d.mixed) {
+        float *f1, *f2, *f3;
+        if ((s = dalloc(&f1, L2 * m)) || (s = dalloc(&f2, L2 * m)) || (s = dalloc(&f3, L2 * m))) { delete c; return s; }
+        d.wA1f = f1; d.wA2f = f2; d.wB2f = f3;
+        if (launch_weights_f32(w1, f1, L2 * m, c->st) != cudaSuccess || launch_weights_f32(w2, f2, L2 * m, c->st) != cudaSuccess ||
+            launch_weights_f32(w3, f3, L2 * m, c->st) != cudaSuccess || cudaStreamSynchronize(c->st) != cudaSuccess) {
+            delete c;
+            return fail(DYN_ERR_CUDA, "FP32 weight copies failed");
+        }
+    }
     if (cudaMallocHost((void**)&c->stages_h, sizeof(StageDev) * SMAX) != cudaSuccess ||
         cudaMallocHost((void**)&c->slots_h, sizeof(Slots)) != cudaSuccess ||
         cudaMallocHost((void**)&c->rhs_h, sizeof(double2) * L) != cudaSuccess) {
@@ -522,6 +567,7 @@ dyn_status dyn_state_init(void* p, double delta_t) {
     dyn_status s = c->upload_times();
     if (s) return s;
     CK(launch_rstep_exact(c->d, 1, c->d.drvec, c->st));
+    if ((s = c->mirror_all())) return s;
     c->ctl.delta_t = delta_t > 0 ? delta_t : c->cfg.delta_t_min;
     c->ctl.loop = 0;
     c->ctl.delta = 1;
@@ -559,6 +605,7 @@ dyn_status dyn_state_upload(void* p, const dyn_state* stt) {
     c->n = n;
     c->t1.assign(stt->t1grid, stt->t1grid + n);
     c->dtr.assign(stt->delta_t_ratio, stt->delta_t_ratio + n);
+    if ((s = c->mirror_all())) return s;
     if ((s = c->upload_times())) return s;
     if ((s = c->pos_init())) return s;
     CK(cudaStreamSynchronize(c->st));
@@ -672,6 +719,7 @@ dyn_status dyn_rhs(void* p, double* hK, double* hR) {
     sp.nrows = (int)c->n;
     sp.n0 = (int)c->n;
     sp.T = c->t1[c->n - 1];
+    Ctx::set_clamps(sp);
     sp.b2_save = NSAVE;  // keep posB2x of the current state readable
     sp.b2_reuse = sp.pos_save = sp.pos_reuse = sp.nb2_save = sp.nb2_reuse = -1;
     dyn_status s = c->pos_init();
@@ -831,6 +879,7 @@ dyn_status dyn_profile_stage(void* p, int reps, float* ms_main, float* ms_epi) {
     sp.nrows = (int)c->n;
     sp.n0 = (int)c->n;
     sp.T = c->t1[c->n - 1];
+    Ctx::set_clamps(sp);
     sp.b2_save = sp.b2_reuse = sp.pos_save = sp.pos_reuse = sp.nb2_save = sp.nb2_reuse = -1;
     dyn_status s = c->pos_init();
     if (s) return s;
@@ -975,6 +1024,7 @@ dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
     c->t1 = t1n;
     c->dtr = dtrn;
     c->n = k;
+    if ((s = c->mirror_all())) return s;
     if ((s = c->upload_times())) return s;
     if ((s = c->pos_init())) return s;
     CK(cudaStreamSynchronize(c->st));

@@ -124,6 +124,15 @@ __device__ __forceinline__ B1Row b1_row(const DevCtx& c, double pos, int maxceil
     return r;
 }
 
+// Position of theta_i * T_next for the next stage (the row written by this
+// stage's epilogue becomes the last list entry), computed while the gather
+// kernel runs so the epilogue only copies it.
+__device__ __forceinline__ void next_position(const DevCtx& c, const StageDev& sp, int i) {
+    if (sp.kind == KIND_RHS || sp.pos_reuse >= 0) return;
+    const ListView lv{c.t1grid, sp.nrows_next, sp.T_next};
+    c.posB1x_next[i] = search_pos(c.search, lv, __dmul_rn(c.theta[i], sp.T_next));
+}
+
 // ------------------------------------------------------------------------
 // k_main: fused gathers + Sigma + convolution products for one stage.
 template <int M, int K, int P, int P2>
@@ -142,7 +151,7 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
     for (int k = threadIdx.x; k < L; k += tpb) s_last[k] = KRl[k];
     if (threadIdx.x == 0) {
         if (live) {
-            const B1Row r = b1_row(c, c.posB1x[i], c.slots->maxceil, nrows);
+            const B1Row r = b1_row(c, c.posB1x[i], sp.maxceil, nrows);
             s_c[0] = r.c0; s_c[1] = r.c1; s_c[2] = r.c2; s_c[3] = r.c3;
             s_bi[0] = r.F; s_bi[1] = r.cubic;
             if (blockIdx.x == 0) {
@@ -164,13 +173,14 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
         }
         if (i == 0 && blockIdx.x == 0) c.slots->q0 = KRl[0].x;
     }
+    if (threadIdx.x == 32 && blockIdx.x == 0) next_position(c, sp, i);
     __syncthreads();
 
     const DModel Mo = c.M;
     const int m = M > 0 ? M : c.m;
     const double bc0 = s_c[0], bc1 = s_c[1], bc2 = s_c[2], bc3 = s_c[3];
     const int F = s_bi[0], cubic1 = s_bi[1];
-    const int maxX = c.slots->maxX;
+    const int maxX = sp.maxX;
     const double2 fill = c.KR[0];
     const ListView lv{c.t1grid, nrows, t};
     const double* pos2_src = sp.b2_reuse >= 0
@@ -268,7 +278,7 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
 
 // ------------------------------------------------------------------------
 // k_epi: RHS, RK combination, history row, r(t), next positions.
-template <int P, int P2>
+template <int P, int P2, bool MIXED>
 __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
     const StageDev& sp = c.stages[s];
     const int L = c.L, tid = threadIdx.x, i = blockIdx.x * EPI_T + tid;
@@ -364,6 +374,10 @@ __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
             const double td = sp.tdiff;
             c.KR[(size_t)sp.n0 * L + i] = g;
             c.dKR[(size_t)sp.n0 * L + i] = make_double2(td * h0.x, td * h0.y);
+            if constexpr (MIXED) {
+                c.KRf[(size_t)sp.n0 * L + i] = make_float2((float)g.x, (float)g.y);
+                c.dKRf[(size_t)sp.n0 * L + i] = make_float2((float)(td * h0.x), (float)(td * h0.y));
+            }
             // rstep (time_steps.cpp:83-92) of the new row at its time
             const double tn = sp.T_next, tw = tn * w;
             double sk, dd;
@@ -375,30 +389,15 @@ __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
                 ep[12] = g.x;
                 ep[13] = sk;
             }
-            // positions of the next stage
-            double pos;
-            if (sp.pos_reuse >= 0) {
-                pos = c.posB1x_saved[(size_t)sp.pos_reuse * L + i];
-            } else {
-                const ListView lv{c.t1grid, sp.nrows_next, tn};
-                pos = search_pos(c.search, lv, __dmul_rn(th, tn));
-            }
+            // positions of the next stage (searched by the gather kernel)
+            const double pos = sp.pos_reuse >= 0 ? c.posB1x_saved[(size_t)sp.pos_reuse * L + i] : c.posB1x_next[i];
             c.posB1x[i] = pos;
             if (sp.pos_save >= 0) c.posB1x_saved[(size_t)sp.pos_save * L + i] = pos;
-            ep[11] = pos;
         }
     }
-    // one warp per CTA: fixed butterfly sums, max for positions
+    // one warp per CTA: fixed butterfly sums
 #pragma unroll
-    for (int k = 0; k < EP_N; ++k) {
-        if (k == 11) {
-            double v = ep[k];
-            for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-            ep[k] = v;
-        } else {
-            ep[k] = warp_sum(ep[k]);
-        }
-    }
+    for (int k = 0; k < EP_N; ++k) ep[k] = warp_sum(ep[k]);
     if (tid < EP_N) {
         double v = 0.0;
 #pragma unroll
@@ -414,9 +413,14 @@ __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
 
     double tot = 0.0;
     if (tid < EP_N) {
-        for (unsigned b = 0; b < gridDim.x; ++b) {
-            const double v = __ldcg(c.epart + (size_t)b * EP_N + tid);
-            tot = tid == 11 ? fmax(tot, v) : tot + v;
+        const unsigned G = gridDim.x;
+        for (unsigned b = 0; b < G; b += 4) {
+            // four independent loads in flight, summed in block order
+            double v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = b + q < G ? __ldcg(c.epart + (size_t)(b + q) * EP_N + tid) : 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tot += v[q];
         }
     }
     __shared__ double s_tot[EP_N];
@@ -434,18 +438,6 @@ __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
         c.t1grid[n0] = sp.T_next;
         c.dtr[n0] = sp.dtr_new;
         c.inv_dtr[n0] = sp.dtr_new != 0.0 ? 1.0 / sp.dtr_new : 0.0;
-        long long mc = (long long)ceil(s_tot[11]) - 1;
-        sl->maxceil = (int)(mc < 1 ? 1 : mc);
-        int mx;
-        if (sp.nb2_reuse >= 0) {
-            mx = sl->saved_maxX[sp.nb2_reuse];
-        } else {
-            const ListView lv{c.t1grid, sp.nrows_next, sp.T_next};
-            const double p = search_pos(c.search, lv, __dmul_rn(c.phi2[(size_t)L * L - 1], sp.T_next));
-            mx = (int)(long long)(p - 0.5);
-        }
-        sl->maxX = mx;
-        if (sp.nb2_save >= 0) sl->saved_maxX[sp.nb2_save] = mx;
         if (sp.last) {
             sl->res_err = s_tot[10];
             sl->res_energy = -(s_tot[1] + s_tot[13] / Mo.T0);
@@ -865,10 +857,13 @@ static cudaError_t launch_main_k(const DevCtx& c, int s, cudaStream_t st) {
 
 template <int P, int P2>
 static cudaError_t launch_stage_pp(const DevCtx& c, int s, cudaStream_t st) {
-    cudaError_t e = c.m == 10 ? launch_main_k<10, P, P2>(c, s, st) : launch_main_k<0, P, P2>(c, s, st);
+    cudaError_t e;
+    if (c.mixed) e = launch_main_mixed(c, s, st);
+    else e = c.m == 10 ? launch_main_k<10, P, P2>(c, s, st) : launch_main_k<0, P, P2>(c, s, st);
     if (e != cudaSuccess) return e;
     const int G = (c.L + EPI_T - 1) / EPI_T;
-    k_epi<P, P2><<<G, EPI_T, 0, st>>>(c, s);
+    if (c.mixed) k_epi<P, P2, true><<<G, EPI_T, 0, st>>>(c, s);
+    else k_epi<P, P2, false><<<G, EPI_T, 0, st>>>(c, s);
     return cudaGetLastError();
 }
 
@@ -884,6 +879,7 @@ static cudaError_t launch_main_pp(const DevCtx& c, int s, cudaStream_t st) {
 }
 
 cudaError_t launch_main_only(const DevCtx& c, int s, cudaStream_t st) {
+    if (c.mixed) return launch_main_mixed(c, s, st);
     if (c.M.p == 3 && c.M.p2 == 4) return launch_main_pp<3, 4>(c, s, st);
     if (c.M.p == 3 && c.M.p2 == 0) return launch_main_pp<3, 0>(c, s, st);
     return launch_main_pp<-1, -1>(c, s, st);
@@ -891,9 +887,15 @@ cudaError_t launch_main_only(const DevCtx& c, int s, cudaStream_t st) {
 
 cudaError_t launch_epi_only(const DevCtx& c, int s, cudaStream_t st) {
     const int G = (c.L + EPI_T - 1) / EPI_T;
-    if (c.M.p == 3 && c.M.p2 == 4) k_epi<3, 4><<<G, EPI_T, 0, st>>>(c, s);
-    else if (c.M.p == 3 && c.M.p2 == 0) k_epi<3, 0><<<G, EPI_T, 0, st>>>(c, s);
-    else k_epi<-1, -1><<<G, EPI_T, 0, st>>>(c, s);
+    if (c.mixed) {
+        if (c.M.p == 3 && c.M.p2 == 4) k_epi<3, 4, true><<<G, EPI_T, 0, st>>>(c, s);
+        else if (c.M.p == 3 && c.M.p2 == 0) k_epi<3, 0, true><<<G, EPI_T, 0, st>>>(c, s);
+        else k_epi<-1, -1, true><<<G, EPI_T, 0, st>>>(c, s);
+    } else {
+        if (c.M.p == 3 && c.M.p2 == 4) k_epi<3, 4, false><<<G, EPI_T, 0, st>>>(c, s);
+        else if (c.M.p == 3 && c.M.p2 == 0) k_epi<3, 0, false><<<G, EPI_T, 0, st>>>(c, s);
+        else k_epi<-1, -1, false><<<G, EPI_T, 0, st>>>(c, s);
+    }
     return cudaGetLastError();
 }
 

@@ -21,7 +21,7 @@ struct StageDev {
     int pos_save, pos_reuse; // epilogue(s): next stage's posB1x save/reuse slot
     int nb2_reuse, nb2_save; // next stage's posB2x flags (for the B2 clamp)
     int ncoef, serk_mode;    // serk_mode: 0 first stage, 1 even, 2 odd
-    int pad0, pad1;
+    int maxceil, maxX;       // B1 Floor clamp and B2 row clamp of this stage (from nrows)
     double T;        // t1grid.back() while this stage's RHS is evaluated
     double T_next;   // time of the row this stage writes
     double tdiff;    // T_next - t1grid[n0-1]
@@ -45,6 +45,7 @@ struct Slots {
 
 struct DevCtx {
     int L, m, nch, search, kpt, tpb;
+    int mixed;             // 1: FP32 gathers/convolutions (dyn_mixed.cu)
     DModel M;
     const double* theta;
     const double* phi2;
@@ -63,6 +64,7 @@ struct DevCtx {
     double* rvec;
     double* drvec;
     double* posB1x;        // [L]
+    double* posB1x_next;   // [L] next stage's positions, written by the gather kernel
     double* posB1x_saved;  // [NSAVE][L]
     double* posB2x;        // [L*L]
     double* posB2x_saved;  // [NSAVE][L*L]
@@ -76,6 +78,12 @@ struct DevCtx {
     Slots* slots;
     StageDev* stages;      // [SMAX]
     double2* rhs_out;      // [L]
+    // mixed form: FP32 copies of the weights and FP32 mirror of the history
+    const float* wA1f;
+    const float* wA2f;
+    const float* wB2f;
+    float2* KRf;
+    float2* dKRf;
     // materialized interpolation (dyn_interpolate)
     double* ip;            // [16][L*L]
     double* rint;          // [L]
@@ -105,6 +113,9 @@ cudaError_t launch_compact(const DevCtx& c, const int* inds, const int* indsD, c
                            cudaStream_t st);
 cudaError_t launch_pack_rows(const double* QK, const double* QR, double2* out, size_t count,
                              cudaStream_t st);
+cudaError_t launch_main_mixed(const DevCtx& c, int s, cudaStream_t st);
+cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cudaStream_t st);
+cudaError_t launch_weights_f32(const double* in, float* out, size_t count, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
 cudaError_t launch_unpack_rows(const double2* in, double* QK, double* QR, size_t count,
                                cudaStream_t st);

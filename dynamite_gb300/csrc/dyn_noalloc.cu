@@ -80,6 +80,8 @@ __global__ void k_noalloc_prep(double* inv, const double* dtr, const double* t1g
         z.nrows = n;
         z.n0 = n;
         z.T = t1grid[n - 1];
+        z.maxceil = n - 1 < 1 ? 1 : n - 1;  // as Ctx::set_clamps
+        z.maxX = n - 1;
         z.b2_save = z.b2_reuse = z.pos_save = z.pos_reuse = z.nb2_save = z.nb2_reuse = -1;
         *sp = z;
         slots->counter = 0;

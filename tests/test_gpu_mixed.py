@@ -1,0 +1,73 @@
+"""Mixed-precision form (FP32 gathers and convolutions with compensated sums;
+r(t), time, C(t,t), the error norm and every O(L) quantity in FP64) against
+the FP64 path and the oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+import dynamite_gb300 as D
+from conftest import load_golden
+from helpers import STATE_FIELDS, grid_from, model_from, rel_err, state_from
+
+pytestmark = pytest.mark.gpu
+
+MIXED_RHS_TOL = 1e-4     # one RHS: a cancelling sum of FP32 terms, relative to max |h|
+MIXED_TRAJ_TOL = 1e-6    # energy / C after a fixed-schedule run, relative
+
+
+@pytest.mark.parametrize("L", [32, 64])
+def test_mixed_rhs_vs_reference(product_built, L):
+    g = load_golden(L)
+    s = D.Simulation(grid_from(g, D.Grid), model_from(g, D.Model), precision="mixed")
+    s.upload(state_from(g, "mid", D.State))
+    hK, hR = s.rhs()
+    assert rel_err(hK, g["mid_qk"]) < MIXED_RHS_TOL
+    assert rel_err(hR, g["mid_qr"]) < MIXED_RHS_TOL
+
+
+@pytest.mark.parametrize("L", [32, 64])
+def test_mixed_trajectory_vs_reference(product_built, L):
+    g = load_golden(L)
+    s = D.Simulation(grid_from(g, D.Grid), model_from(g, D.Model), precision="mixed")
+    s.init()
+    tr = s.run(g["traj_dt"].size, schedule=(g["traj_dt"], g["traj_method"]))
+    st = s.download()
+    np.testing.assert_array_equal(st.t1grid, g["traj_final_t1grid"])  # time stays FP64
+    assert rel_err(tr["energy"], g["traj_energy"]) < MIXED_TRAJ_TOL
+    assert rel_err(st.QK, g["traj_final_QK"]) < MIXED_TRAJ_TOL
+    assert rel_err(st.rvec, g["traj_final_rvec"]) < MIXED_TRAJ_TOL
+
+
+def test_mixed_large_grid_vs_fp64(product_built):
+    """L=512, the FP64 run's schedule replayed in mixed precision."""
+    L = 512
+    grid = D.grid.generate(L)
+    m = D.Model(p=3, p2=4, lam=0.5, Gamma=0.6)
+    a = D.Simulation(grid, m)
+    b = D.Simulation(grid, m, precision="mixed")
+    a.init()
+    b.init()
+    ta = a.run(300)
+    tb = b.run(300, schedule=(ta["dt"], ta["method"]))
+    sa, sb = a.download(), b.download()
+    np.testing.assert_array_equal(sa.t1grid, sb.t1grid)
+    assert rel_err(tb["energy"], ta["energy"]) < MIXED_TRAJ_TOL
+    assert rel_err(sb.QK, sa.QK) < MIXED_TRAJ_TOL
+    assert rel_err(sb.rvec, sa.rvec) < MIXED_TRAJ_TOL
+    # C(t,t) (theta = 1 column) stays at its FP64 value to within the FP64 error
+    L_ = L
+    diag_a = sa.QK.reshape(-1, L_)[:, -1]
+    diag_b = sb.QK.reshape(-1, L_)[:, -1]
+    assert np.max(np.abs(diag_a - diag_b)) < 1e-6
+
+
+def test_mixed_sparsify_and_graph_replay(product_built):
+    g = load_golden(32)
+    s = D.Simulation(grid_from(g, D.Grid), model_from(g, D.Model), precision="mixed", use_graph=True)
+    s.upload(state_from(g, "traj_final", D.State))
+    n = s.sparsifyNscale(float(g["spars_threshold"][0]), "gpu")
+    assert n < g["traj_final_t1grid"].size
+    dt = float(g["traj_dt"][-1])
+    r1 = s.update(1, dt)
+    r2 = s.update(1, dt)
+    assert np.isfinite([r1.delta, r2.delta, r2.energy]).all()
