@@ -163,7 +163,8 @@ struct Ctx {
                         (void*)d.wA1, (void*)d.wA2, (void*)d.wB2, d.KR, d.dKR, d.t1grid, d.dtr, d.inv_dtr,
                         d.rvec, d.drvec, d.posB1x, d.posB1x_next, d.posB1x_saved, d.posB2x, d.posB2x_saved, d.h, d.gS,
                         d.geS, d.gfS, d.part, d.rowval, d.epart, d.slots, d.stages, d.rhs_out, d.ip,
-                        d.rint, scratch_dev, (void*)d.wA1f, (void*)d.wA2f, (void*)d.wB2f, d.KRf, d.dKRf};
+                        d.rint, scratch_dev, (void*)d.wA1f, (void*)d.wA2f, (void*)d.wB2f, d.KRf, d.dKRf,
+                        (void*)d.integ_f, d.inv_len_f, d.inv_dtr_f};
         for (void* b : bufs) if (b) cudaFree(b);
         std::memset(&d, 0, sizeof d);
         scratch_dev = nullptr;
@@ -194,6 +195,8 @@ struct Ctx {
             (s = dalloc(&dt, ncap)) || (s = dalloc(&idt, ncap)) || (s = dalloc(&rv, ncap)) || (s = dalloc(&drv, ncap)))
             return s;
         float2 *KRf = nullptr, *dKRf = nullptr;
+        float *ilen = nullptr, *idtf = nullptr;
+        if (d.mixed && ((s = dalloc(&ilen, ncap)) || (s = dalloc(&idtf, ncap)))) return s;
         // +16 elements: the 16-byte segment loads of the mixed kernel may touch
         // one element past the end of the last row
         if (d.mixed && ((s = dalloc(&KRf, ncap * L + 16)) || (s = dalloc(&dKRf, ncap * L + 16)))) return s;
@@ -218,8 +221,13 @@ struct Ctx {
         if (d.mixed) {
             if (d.KRf) cudaFree(d.KRf);
             if (d.dKRf) cudaFree(d.dKRf);
+            if (d.inv_len_f) cudaFree(d.inv_len_f);
+            if (d.inv_dtr_f) cudaFree(d.inv_dtr_f);
             d.KRf = KRf;
             d.dKRf = dKRf;
+            d.inv_len_f = ilen;
+            d.inv_dtr_f = idtf;
+            if (n) CK(launch_time_f32(d.t1grid, d.dtr, (int)n, d.inv_len_f, d.inv_dtr_f, st));
         }
         cap = ncap;
         drop_graphs();
@@ -232,6 +240,7 @@ struct Ctx {
         CK(cudaMemcpyAsync(d.t1grid, t1.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(d.dtr, dtr.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(d.inv_dtr, inv.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+        if (d.mixed) CK(launch_time_f32(d.t1grid, d.dtr, (int)n, d.inv_len_f, d.inv_dtr_f, st));
         CK(cudaStreamSynchronize(st));
         return DYN_OK;
     }
@@ -485,7 +494,7 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     M.Gamma = cfg->Gamma;
 
     dyn_status s;
-    const int G = (int)((L + EPI_T - 1) / EPI_T);
+    const int G = (int)((L + EPI_ROWS - 1) / EPI_ROWS);
     double *th, *p2, *it, *w1, *w2, *w3;
     int *a1, *a2, *b2;
     if ((s = dalloc(&th, L)) || (s = dalloc(&p2, L2)) || (s = dalloc(&it, L)) || (s = dalloc(&a1, L2)) ||
@@ -518,6 +527,10 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
         float *f1, *f2, *f3;
         if ((s = dalloc(&f1, L2 * m)) || (s = dalloc(&f2, L2 * m)) || (s = dalloc(&f3, L2 * m))) { delete c; return s; }
         d.wA1f = f1; d.wA2f = f2; d.wB2f = f3;
+        float* itf;
+        if ((s = dalloc(&itf, L))) { delete c; return s; }
+        d.integ_f = itf;
+        if (launch_weights_f32(it, itf, L, c->st) != cudaSuccess) { delete c; return fail(DYN_ERR_CUDA, "FP32 int.dat copy failed"); }
         if (launch_weights_f32(w1, f1, L2 * m, c->st) != cudaSuccess || launch_weights_f32(w2, f2, L2 * m, c->st) != cudaSuccess ||
             launch_weights_f32(w3, f3, L2 * m, c->st) != cudaSuccess || cudaStreamSynchronize(c->st) != cudaSuccess) {
             delete c;

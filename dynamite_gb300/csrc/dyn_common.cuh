@@ -174,6 +174,12 @@ __device__ __forceinline__ int warp_reduce8_index(int lane) {
     return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization starts while its predecessor drains; this waits until the
+// predecessor has finished and its writes are visible.  Without a
+// programmatic edge it returns at once.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

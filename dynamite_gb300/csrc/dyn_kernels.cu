@@ -137,6 +137,7 @@ __device__ __forceinline__ void next_position(const DevCtx& c, const StageDev& s
 // k_main: fused gathers + Sigma + convolution products for one stage.
 template <int M, int K, int P, int P2>
 __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
+    wait_prior_grid();
     const StageDev& sp = c.stages[s];
     const int L = c.L, tpb = blockDim.x, i = blockIdx.y;
     const int nrows = sp.nrows;
@@ -280,15 +281,16 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
 // k_epi: RHS, RK combination, history row, r(t), next positions.
 template <int P, int P2, bool MIXED>
 __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
+    wait_prior_grid();
     const StageDev& sp = c.stages[s];
-    const int L = c.L, tid = threadIdx.x, i = blockIdx.x * EPI_T + tid;
+    const int L = c.L, tid = threadIdx.x, i = blockIdx.x * EPI_ROWS + tid;
     const DModel Mo = c.M;
     double ep[EP_N];
 #pragma unroll
     for (int k = 0; k < EP_N; ++k) ep[k] = 0.0;
     __shared__ int s_is_last;
 
-    if (i < L) {
+    if (tid < EPI_ROWS && i < L) {
         double a[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) a[k] = 0.0;
@@ -395,9 +397,21 @@ __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
             if (sp.pos_save >= 0) c.posB1x_saved[(size_t)sp.pos_save * L + i] = pos;
         }
     }
-    // one warp per CTA: fixed butterfly sums
+    // one warp per CTA: fixed butterfly sums of the quantities this stage uses
+    // (r(t) always; dr/dt at stage 0; error norm and C(t,0), f'(C(t,0)) at the last)
+    if (sp.kind != KIND_RHS) {
 #pragma unroll
-    for (int k = 0; k < EP_N; ++k) ep[k] = warp_sum(ep[k]);
+        for (int k = 0; k < 3; ++k) ep[k] = warp_sum(ep[k]);
+        if (s == 0) {
+#pragma unroll
+            for (int k = 3; k < 10; ++k) ep[k] = warp_sum(ep[k]);
+        }
+        if (sp.last) {
+            ep[10] = warp_sum(ep[10]);
+            ep[12] = warp_sum(ep[12]);
+            ep[13] = warp_sum(ep[13]);
+        }
+    }
     if (tid < EP_N) {
         double v = 0.0;
 #pragma unroll
@@ -438,6 +452,10 @@ __global__ void __launch_bounds__(EPI_T) k_epi(const DevCtx c, const int s) {
         c.t1grid[n0] = sp.T_next;
         c.dtr[n0] = sp.dtr_new;
         c.inv_dtr[n0] = sp.dtr_new != 0.0 ? 1.0 / sp.dtr_new : 0.0;
+        if constexpr (MIXED) {
+            c.inv_dtr_f[n0] = sp.dtr_new != 0.0 ? (float)(1.0 / sp.dtr_new) : 0.0f;
+            c.inv_len_f[n0 - 1] = (float)(1.0 / sp.tdiff);
+        }
         if (sp.last) {
             sl->res_err = s_tot[10];
             sl->res_energy = -(s_tot[1] + s_tot[13] / Mo.T0);
@@ -842,8 +860,7 @@ static cudaError_t launch_main_t(const DevCtx& c, int s, cudaStream_t st) {
         cudaFuncSetAttribute(k_main<M, K, P, P2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         attr_set = true;
     }
-    k_main<M, K, P, P2><<<grid, block, smem, st>>>(c, s);
-    return cudaGetLastError();
+    return launch_pdl(k_main<M, K, P, P2>, grid, block, smem, st, c, s);
 }
 
 template <int M, int P, int P2>
@@ -861,10 +878,9 @@ static cudaError_t launch_stage_pp(const DevCtx& c, int s, cudaStream_t st) {
     if (c.mixed) e = launch_main_mixed(c, s, st);
     else e = c.m == 10 ? launch_main_k<10, P, P2>(c, s, st) : launch_main_k<0, P, P2>(c, s, st);
     if (e != cudaSuccess) return e;
-    const int G = (c.L + EPI_T - 1) / EPI_T;
-    if (c.mixed) k_epi<P, P2, true><<<G, EPI_T, 0, st>>>(c, s);
-    else k_epi<P, P2, false><<<G, EPI_T, 0, st>>>(c, s);
-    return cudaGetLastError();
+    const int G = (c.L + EPI_ROWS - 1) / EPI_ROWS;
+    if (c.mixed) return launch_pdl(k_epi<P, P2, true>, dim3(G), dim3(EPI_T), 0, st, c, s);
+    return launch_pdl(k_epi<P, P2, false>, dim3(G), dim3(EPI_T), 0, st, c, s);
 }
 
 cudaError_t launch_stage(const DevCtx& c, int s, cudaStream_t st) {
@@ -886,7 +902,7 @@ cudaError_t launch_main_only(const DevCtx& c, int s, cudaStream_t st) {
 }
 
 cudaError_t launch_epi_only(const DevCtx& c, int s, cudaStream_t st) {
-    const int G = (c.L + EPI_T - 1) / EPI_T;
+    const int G = (c.L + EPI_ROWS - 1) / EPI_ROWS;
     if (c.mixed) {
         if (c.M.p == 3 && c.M.p2 == 4) k_epi<3, 4, true><<<G, EPI_T, 0, st>>>(c, s);
         else if (c.M.p == 3 && c.M.p2 == 0) k_epi<3, 0, true><<<G, EPI_T, 0, st>>>(c, s);

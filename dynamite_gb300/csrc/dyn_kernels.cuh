@@ -8,7 +8,9 @@ namespace dyn {
 
 constexpr int SMAX = 32;      // most stages of one step (SERK2 with q <= 16)
 constexpr int NSAVE = 3;      // SSPRK(10,4) keeps positions of stages 2..4
-constexpr int EPI_T = 32;     // rows per epilogue CTA
+constexpr int EPI_T = 32;     // threads per epilogue CTA (one warp)
+constexpr int EPI_ROWS = 32;  // rows per epilogue CTA (one row per lane; spreading rows over
+                              // more SMs did not shorten its FP64 dependency chain)
 constexpr int EP_N = 16;      // per-CTA epilogue partials
 
 enum StageKind { KIND_TABLEAU = 0, KIND_SERK = 1, KIND_RHS = 2 };
@@ -84,10 +86,31 @@ struct DevCtx {
     const float* wB2f;
     float2* KRf;
     float2* dKRf;
+    const float* integ_f;  // [L]   int.dat in FP32
+    float* inv_dtr_f;      // [cap] 1/delta_t_ratio in FP32
+    float* inv_len_f;      // [cap] 1/(t1grid[k+1]-t1grid[k]) in FP32
     // materialized interpolation (dyn_interpolate)
     double* ip;            // [16][L*L]
     double* rint;          // [L]
 };
+
+// Launch with programmatic stream serialization (overlaps the launch with the
+// previous kernel's tail; the kernel itself calls wait_prior_grid first).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
 
 // launch wrappers (dyn_kernels.cu)
 cudaError_t launch_stage(const DevCtx& c, int s, cudaStream_t st);
@@ -116,6 +139,8 @@ cudaError_t launch_pack_rows(const double* QK, const double* QR, double2* out, s
 cudaError_t launch_main_mixed(const DevCtx& c, int s, cudaStream_t st);
 cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cudaStream_t st);
 cudaError_t launch_weights_f32(const double* in, float* out, size_t count, cudaStream_t st);
+cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr,
+                            cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
 cudaError_t launch_unpack_rows(const double2* in, double* QK, double* QR, size_t count,
                                cudaStream_t st);

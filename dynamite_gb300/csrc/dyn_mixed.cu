@@ -10,7 +10,9 @@
 //     r(t), dr/dt, C(t,t), the step-error norm, time) stay in FP64.
 // The position search is the exact FP64 binary search (integer compares on
 // the bit patterns); only the fractional offset inside the located interval
-// is formed in FP32, so interval indices equal the FP64 form's.
+// is formed in FP32 (one FP64 difference scaled by a stored FP32 inverse
+// interval length), so interval indices equal the FP64 form's.  FP32 copies
+// of int.dat and 1/delta_t_ratio keep conversions off the (slow) FP64 pipe.
 #include <cmath>
 #include "dyn_kernels.cuh"
 
@@ -106,6 +108,38 @@ __device__ __forceinline__ float2 seg10(const float w[10], const float2* __restr
     return acc;
 }
 
+// The same 10-tap segment from shared memory (the staged last row)
+__device__ __forceinline__ float2 seg10s(const float w[10], const float2* arr, int b) {
+    const int a = b & ~1;
+    const bool sh = b & 1;
+    const float4* p = reinterpret_cast<const float4*>(arr + a);
+    float2 e[12];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float4 v = p[k];
+        e[2 * k] = make_float2(v.x, v.y);
+        e[2 * k + 1] = make_float2(v.z, v.w);
+    }
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 10; ++d) {
+        const float2 x = sh ? e[d + 1] : e[d];
+        acc.x = fmaf(w[d], x.x, acc.x);
+        acc.y = fmaf(w[d], x.y, acc.y);
+    }
+    return acc;
+}
+
+__device__ __forceinline__ void load_w10(const float* w, float wv[10]) {
+    const float2* w2 = reinterpret_cast<const float2*>(w);
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+        const float2 q = __ldg(w2 + d);
+        wv[2 * d] = q.x;
+        wv[2 * d + 1] = q.y;
+    }
+}
+
 // TwoSum accumulation: s + c carries the sum to about twice FP32 precision
 __device__ __forceinline__ void two_sum_add(float& s, float& c, float v) {
     const float t = s + v;
@@ -156,7 +190,8 @@ __device__ __forceinline__ void warp_reduce8_pair(const float hv[8], const float
 
 // Binary search of bsearchPosSorted (the same probes as pos_binary), returning
 // floor(position) as an integer and the offset from it in FP32.
-__device__ __forceinline__ void pos_split(const ListView& L, double El, long long& X, float& x) {
+__device__ __forceinline__ void pos_split(const ListView& L, const float* __restrict__ inv_len, double El,
+                                          long long& X, float& x) {
     int n0 = 1, n1 = L.n, m = 1;
     double Lm = 0.0;
     const long long kE = okey(El);
@@ -171,12 +206,14 @@ __device__ __forceinline__ void pos_split(const ListView& L, double El, long lon
     }
     if (okey(Lm) <= kE) {
         if (m == L.n) { X = m; x = 0.f; return; }
-        const float f = (float)(El - Lm) / (float)(L.at(m) - Lm);
+        // interval [list[m-1], list[m]]: one FP64 difference, FP32 scale
+        const float f = (float)(El - Lm) * __ldg(inv_len + (m - 1));
         if (f >= 1.0f) { X = m + 1; x = f - 1.0f; } else { X = m; x = f; }
         return;
     }
     if (m > 1) {
-        const float f = (float)(El - Lm) / (float)(L.at(m - 2) - Lm);  // position m - f
+        // interval [list[m-2], list[m-1]], position m - f
+        const float f = (float)(Lm - El) * __ldg(inv_len + (m - 2));
         if (f > 0.0f) { X = m - 1; x = 1.0f - f; } else { X = m; x = -f; }
         return;
     }
@@ -188,6 +225,7 @@ __device__ __forceinline__ void pos_split(const ListView& L, double El, long lon
 
 template <int M, int K, int P, int P2>
 __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s) {
+    wait_prior_grid();
     const StageDev& sp = c.stages[s];
     const int L = c.L, tpb = blockDim.x, i = blockIdx.y;
     const int nrows = sp.nrows;
@@ -200,6 +238,7 @@ __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s)
 
     const float2* KRl = c.KRf + (size_t)(nrows - 1) * L;
     for (int k = threadIdx.x; k < L; k += tpb) s_lastf[k] = KRl[k];
+    if (threadIdx.x == 0) s_lastf[L] = make_float2(0.f, 0.f), s_lastf[L + 1] = make_float2(0.f, 0.f);
     if (threadIdx.x == 0) {
         if (live) {
             // row constants in FP64 from the master history (as k_main)
@@ -261,8 +300,16 @@ __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s)
             const size_t ij = (size_t)i * L + j;
             float2 a1, a2, b1, b2;
             if (live) {
-                a1 = dotf<M>(c.wA1f + ij * m, s_lastf + __ldg(c.iA1 + ij), m, false);
-                a2 = dotf<M>(c.wA2f + ij * m, s_lastf + __ldg(c.iA2 + ij), m, false);
+                if constexpr (M == 10) {
+                    float wv[10];
+                    load_w10(c.wA1f + ij * 10, wv);
+                    a1 = seg10s(wv, s_lastf, __ldg(c.iA1 + ij));
+                    load_w10(c.wA2f + ij * 10, wv);
+                    a2 = seg10s(wv, s_lastf, __ldg(c.iA2 + ij));
+                } else {
+                    a1 = dotf<M>(c.wA1f + ij * m, s_lastf + __ldg(c.iA1 + ij), m, false);
+                    a2 = dotf<M>(c.wA2f + ij * m, s_lastf + __ldg(c.iA2 + ij), m, false);
+                }
                 {
                     const float2 x0 = __ldg(c.KRf + (size_t)(F - 1) * L + j);
                     const float2 x1 = __ldg(c.KRf + (size_t)F * L + j);
@@ -278,7 +325,7 @@ __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s)
                 {
                     long long X;
                     float x;
-                    pos_split(lv, __dmul_rn(__ldg(c.phi2 + ij), t), X, x);
+                    pos_split(lv, c.inv_len_f, __dmul_rn(__ldg(c.phi2 + ij), t), X, x);
                     if (X > maxX) { x += (float)(X - maxX); X = maxX; }
                     if (X < 1) { x -= (float)(1 - X); X = 1; }
                     const float x2 = x * x, x3 = x2 * x;
@@ -308,7 +355,7 @@ __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s)
                     if (cubic2) {
                         const float e0 = 1.f - 3.f * x2 + 2.f * x3, e1 = x - 2.f * x2 + x3;
                         const float e2 = 3.f * x2 - 2.f * x3;
-                        const float e3 = (x3 - x2) * (float)c.inv_dtr[X + 1];
+                        const float e3 = (x3 - x2) * __ldg(c.inv_dtr_f + X + 1);
                         b2.x = e0 * S0.x + e1 * D1.x + e2 * S1.x + e3 * D2.x;
                         b2.y = e0 * S0.y + e1 * D1.y + e2 * S1.y + e3 * D2.y;
                     } else {
@@ -328,7 +375,7 @@ __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s)
             const float sRB1 = dB1 * b1.y;
             SigF<P, P2>::d12(Mf, b2.x, sKB2, dB2);
             const float sRB2 = dB2 * b2.y;
-            const float wj = (float)__ldg(c.integ + j);
+            const float wj = __ldg(c.integ_f + j);
             const float wRA2 = wj * sRA2, wQRA2 = wj * a2.y;
             two_sum_add(acc[0], cmp[0], wRA2 * b2.x);
             two_sum_add(acc[1], cmp[1], (wj * sRA1) * b1.x);
@@ -357,8 +404,7 @@ namespace {
 template <int M, int K, int P, int P2>
 cudaError_t launch_t(const DevCtx& c, int s, cudaStream_t st) {
     dim3 grid(c.nch, c.L), block(c.tpb);
-    k_main_mixed<M, K, P, P2><<<grid, block, (size_t)c.L * sizeof(float2), st>>>(c, s);
-    return cudaGetLastError();
+    return launch_pdl(k_main_mixed<M, K, P, P2>, grid, block, (size_t)(c.L + 2) * sizeof(float2), st, c, s);
 }
 
 template <int M, int P, int P2>
@@ -382,6 +428,14 @@ __global__ void k_to_f32(const double2* in, float2* out, size_t count) {
     }
 }
 
+// FP32 inverse interval lengths and inverse step ratios of rows [0, n)
+__global__ void k_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        inv_dtr[k] = dtr[k] != 0.0 ? (float)(1.0 / dtr[k]) : 0.0f;
+        inv_len[k] = k + 1 < n ? (float)(1.0 / (t1[k + 1] - t1[k])) : 0.0f;
+    }
+}
+
 __global__ void k_weights_f32(const double* in, float* out, size_t count) {
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
         out[e] = (float)in[e];
@@ -398,6 +452,12 @@ cudaError_t launch_main_mixed(const DevCtx& c, int s, cudaStream_t st) {
 cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cudaStream_t st) {
     const int blocks = (int)((count + 255) / 256 < 8192 ? (count + 255) / 256 : 8192);
     k_to_f32<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr,
+                            cudaStream_t st) {
+    k_time_f32<<<(n + 255) / 256, 256, 0, st>>>(t1, dtr, n, inv_len, inv_dtr);
     return cudaGetLastError();
 }
 

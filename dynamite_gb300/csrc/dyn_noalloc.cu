@@ -40,7 +40,7 @@ constexpr int MAX_LEN = DYN_NOALLOC_MAX_LEN;
 constexpr int MAX_ROWS = DYN_NOALLOC_MAX_ROWS;
 constexpr int TPB = 64;
 constexpr int MAX_NCH = 4;  // chunks per row for the tile shapes chosen below (<= 4 for len <= 1024)
-constexpr int MAX_G = (MAX_LEN + EPI_T - 1) / EPI_T;
+constexpr int MAX_G = (MAX_LEN + EPI_ROWS - 1) / EPI_ROWS;
 
 // scratch layout, in doubles
 constexpr size_t OFF_PART = 0;
