@@ -81,6 +81,35 @@ class NoAllocRHS(C.Structure):
     ]
 
 
+class BatchGrid(C.Structure):
+    _fields_ = [("len", C.c_size_t), ("depth", C.c_size_t), ("tables", Tables)]
+
+
+class BatchQuench(C.Structure):
+    _fields_ = [
+        ("grid", C.c_int), ("p", C.c_int), ("p2", C.c_int), ("lam", C.c_double), ("T0", C.c_double),
+        ("Gamma", C.c_double), ("delta_t_min", C.c_double), ("delta_max", C.c_double), ("delta_t", C.c_double),
+        ("t_stop", C.c_double), ("max_steps", C.c_longlong), ("capacity", C.c_size_t),
+    ]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [
+        ("device", C.c_int), ("stream", C.c_void_p), ("search", C.c_int), ("gpu_rollback", C.c_int),
+        ("ticks_per_launch", C.c_int), ("threads", C.c_int), ("targets", C.c_int), ("ctas_per_sm", C.c_int),
+    ]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("method", C.c_int), ("loop", C.c_int), ("pad", C.c_int), ("steps", C.c_longlong),
+        ("n", C.c_size_t), ("t", C.c_double), ("delta_t", C.c_double), ("delta", C.c_double),
+        ("delta_old", C.c_double), ("energy", C.c_double), ("r", C.c_double), ("qk0", C.c_double),
+    ]
+
+
+DYN_QUENCH_RUNNING, DYN_QUENCH_DONE, DYN_QUENCH_MAXSTEPS, DYN_QUENCH_FULL = 0, 1, 2, 3
+
 _lib = None
 
 
@@ -125,6 +154,16 @@ def lib():
             "dyn_profile_stage": ([vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
             "dyn_probe_fp64": ([C.c_int, dp], C.c_int),
             "dyn_rhs_noalloc": ([C.POINTER(NoAllocRHS), vp], C.c_int),
+            "dyn_batch_create": ([C.POINTER(BatchConfig), C.POINTER(BatchGrid), C.c_int, C.POINTER(BatchQuench),
+                                  C.c_int, C.POINTER(vp)], C.c_int),
+            "dyn_batch_destroy": ([vp], C.c_int),
+            "dyn_batch_upload": ([vp, C.c_int, C.POINTER(StateC), C.POINTER(Controller)], C.c_int),
+            "dyn_batch_download": ([vp, C.c_int, C.POINTER(StateC)], C.c_int),
+            "dyn_batch_get_info": ([vp, C.c_int, C.POINTER(BatchInfo)], C.c_int),
+            "dyn_batch_set_limits": ([vp, C.c_int, C.c_double, C.c_longlong], C.c_int),
+            "dyn_batch_run": ([vp, C.c_longlong, C.POINTER(C.c_longlong)], C.c_int),
+            "dyn_batch_tune": ([vp, C.c_int, ip, ip, ip, C.POINTER(C.c_float)], C.c_int),
+            "dyn_batch_profile": ([vp, C.c_int, C.POINTER(C.c_float)], C.c_int),
             "dyn_grid_generate": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                    dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
         }

@@ -57,7 +57,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     dig = _digest(deps) + os.uname().machine
     if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == dig:
         return LIB
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", f"-I{INCLUDE}"]
+    # host code: IEEE arithmetic as written (no FMA contraction on any host ISA), so the
+    # host-side time grid matches the reference's -ffp-contract=off build everywhere
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off",
+              f"-I{INCLUDE}"]
     jobs = []
     for s in cu:
         obj = os.path.join(OUT, s + ".o")

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/dyn.h"
+#include "dyn_host.h"
 #include "dyn_kernels.cuh"
 
 using namespace dyn;
@@ -35,90 +36,6 @@ dyn_status fail(dyn_status s, const std::string& msg) {
         if (e_ != cudaSuccess)                                                                \
             return fail(DYN_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
     } while (0)
-
-const double RMAX[11] = {3, 13, 20, 80, 180, 320, 500, 720, 980, 1280, 1620};
-
-// Dormand-Prince tableau (runge_kutta.cpp:149-159)
-const double RK54_A[7][7] = {
-    {0, 0, 0, 0, 0, 0, 0},
-    {1.0 / 5, 0, 0, 0, 0, 0, 0},
-    {3.0 / 40, 9.0 / 40, 0, 0, 0, 0, 0},
-    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0, 0},
-    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0, 0},
-    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0, 0},
-    {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84, 0}};
-const double RK54_B[7] = {35.0 / 384, 0.0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84, 0.0};
-const double RK54_B2[7] = {5179.0 / 57600, 0.0, 7571.0 / 16695, 393.0 / 640, -92097.0 / 339200, 187.0 / 2100, 1.0 / 40};
-
-// SSPRK(10,4) tableau (runge_kutta.cpp:22-35)
-double ssp_a(int r, int c) {
-    if (c >= r) return 0.0;
-    return (r <= 4 || c >= 5) ? 1.0 / 6 : 1.0 / 15;
-}
-const double SSP_B[10] = {1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10, 1.0 / 10};
-const double SSP_B2[10] = {0., 2.0 / 9, 0, 0, 5.0 / 18, 1.0 / 3, 0., 0., 0., 1.0 / 6};
-
-// SERK2 coefficients (runge_kutta.cu:202-272), long double solve
-long double chebT(int n, long double x) {
-    if (n == 0) return 1.0L;
-    if (n == 1) return x;
-    long double t0 = 1.0L, t1 = x;
-    for (int i = 2; i <= n; ++i) { long double t2 = 2.0L * x * t1 - t0; t0 = t1; t1 = t2; }
-    return t1;
-}
-long double chebU(int n, long double x) {
-    if (n == 0) return 1.0L;
-    if (n == 1) return 2.0L * x;
-    long double u0 = 1.0L, u1 = 2.0L * x;
-    for (int i = 2; i <= n; ++i) { long double u2 = 2.0L * x * u1 - u0; u0 = u1; u1 = u2; }
-    return u1;
-}
-std::vector<double> serk_coeffs(int q) {
-    const int mm = 2, s = mm * q, N = s + 1;
-    const long double mup = 19.0L / 20.0L;
-    const long double a2 = (long double)q / ((long double)s * s);
-    const long double w0 = 1.0L + mup / ((long double)s * s);
-    const long double w1 = chebT(s, w0) / ((long double)s * chebU(s - 1, w0));
-    std::vector<std::vector<long double>> A(N, std::vector<long double>(N + 1, 0.0L));
-    for (int zi = 0; zi < N; ++zi) {
-        const long double z = (long double)(zi + 1);
-        A[zi][N] = chebT(s, w0 + w1 * z) / chebT(s, w0);
-        A[zi][0] = chebT(0, 1.0L + a2 * z);
-        for (int j = 1; j <= q; ++j) {
-            const long double tmj = std::pow(chebT(mm, 1.0L + a2 * z), j - 1);
-            for (int i = 1; i <= mm; ++i) A[zi][i + mm * (j - 1)] = chebT(i, 1.0L + a2 * z) * tmj;
-        }
-    }
-    for (int i = 0; i < N; ++i) {
-        int mx = i;
-        for (int k = i + 1; k < N; ++k) if (std::fabs(A[k][i]) > std::fabs(A[mx][i])) mx = k;
-        std::swap(A[i], A[mx]);
-        for (int k = i + 1; k < N; ++k) {
-            const long double f = A[k][i] / A[i][i];
-            for (int j = i; j <= N; ++j) A[k][j] -= f * A[i][j];
-        }
-    }
-    std::vector<long double> x(N);
-    for (int i = N - 1; i >= 0; --i) {
-        x[i] = A[i][N];
-        for (int j = i + 1; j < N; ++j) x[i] -= A[i][j] * x[j];
-        x[i] /= A[i][i];
-    }
-    std::vector<double> out(N);
-    for (int i = 0; i < N; ++i) out[i] = (double)x[i];
-    return out;
-}
-
-double pow_int_h(double b, int e) {
-    if (e == 0) return 1.0;
-    if (e == 1) return b;
-    if (e == 2) return b * b;
-    if (e == 3) return b * b * b;
-    if (e == 4) { double sq = b * b; return sq * sq; }
-    double r = 1.0, c = b;
-    while (e > 0) { if (e & 1) r *= c; c *= c; e >>= 1; }
-    return r;
-}
 
 template <typename T>
 dyn_status dalloc(T** p, size_t count) {
@@ -176,13 +93,8 @@ struct Ctx {
         st = nullptr;
     }
 
-    double Df_h(double q) const {
-        return cfg.lambda * cfg.p * pow_int_h(q, cfg.p - 1) + (1 - cfg.lambda) * cfg.p2 * pow_int_h(q, cfg.p2 - 1);
-    }
-    double DDf_h(double q) const {
-        return cfg.lambda * cfg.p * (cfg.p - 1) * pow_int_h(q, cfg.p - 2) +
-               (1 - cfg.lambda) * cfg.p2 * (cfg.p2 - 1) * pow_int_h(q, cfg.p2 - 2);
-    }
+    double Df_h(double q) const { return Df_host(cfg.lambda, cfg.p, cfg.p2, q); }
+    double DDf_h(double q) const { return DDf_host(cfg.lambda, cfg.p, cfg.p2, q); }
 
     dyn_status ensure_rows(size_t rows) {
         if (rows <= cap) return DYN_OK;
@@ -265,12 +177,6 @@ struct Ctx {
     static void set_clamps(StageDev& sp) {
         sp.maxceil = sp.nrows - 1 < 1 ? 1 : sp.nrows - 1;
         sp.maxX = sp.nrows - 1;
-    }
-
-    int stages_of(int method) const {
-        if (method == DYN_RK54) return 7;
-        if (method == DYN_SSPRK104) return 10;
-        return 2 * (2 * (method - 2));
     }
 
     // Fill stages_h for one step; returns the host-side part of the error
@@ -422,6 +328,88 @@ Ctx* C(void* p) { return static_cast<Ctx*>(p); }
 
 namespace dyn {
 void set_last_error(const std::string& msg) { g_err = msg; }
+
+// The checks every table set passes before it reaches the device: theta
+// non-decreasing on [0, 1] with theta[L-1] == 1, phi2 in [0, 1] ending at 1
+// (these make the largest search position the last row, so the B1/B2 clamps
+// are known on the host), stencil starts in [0, L-m]; the starts come back
+// as int32.
+bool check_tables(size_t L, size_t m, const dyn_tables* tb, std::vector<int> i32[3], std::string& why) {
+    if (!tb->theta || !tb->phi2 || !tb->integ || !tb->indsA1y || !tb->indsA2y || !tb->indsB2y || !tb->weightsA1y ||
+        !tb->weightsA2y || !tb->weightsB2y) {
+        why = "missing table";
+        return false;
+    }
+    for (size_t i = 1; i < L; ++i)
+        if (!(tb->theta[i] >= tb->theta[i - 1])) { why = "theta must be non-decreasing"; return false; }
+    if (tb->theta[0] < 0.0 || tb->theta[L - 1] != 1.0) { why = "theta must span [0, 1]"; return false; }
+    const size_t L2 = L * L;
+    const int64_t* src[3] = {tb->indsA1y, tb->indsA2y, tb->indsB2y};
+    for (int k = 0; k < 3; ++k) {
+        i32[k].resize(L2);
+        for (size_t e = 0; e < L2; ++e) {
+            const int64_t v = src[k][e];
+            if (v < 0 || (size_t)v + m > L) { why = "stencil start out of range [0, len-depth]"; return false; }
+            i32[k][e] = (int)v;
+        }
+    }
+    for (size_t e = 0; e < L2; ++e)
+        if (!(tb->phi2[e] >= 0.0 && tb->phi2[e] <= 1.0)) { why = "phi2 outside [0, 1]"; return false; }
+    if (tb->phi2[L2 - 1] != 1.0) { why = "phi2 must end at 1"; return false; }
+    return true;
+}
+
+// SERK2 coefficients (runge_kutta.cu:202-272), long double solve
+static long double chebT(int n, long double x) {
+    if (n == 0) return 1.0L;
+    if (n == 1) return x;
+    long double t0 = 1.0L, t1 = x;
+    for (int i = 2; i <= n; ++i) { long double t2 = 2.0L * x * t1 - t0; t0 = t1; t1 = t2; }
+    return t1;
+}
+static long double chebU(int n, long double x) {
+    if (n == 0) return 1.0L;
+    if (n == 1) return 2.0L * x;
+    long double u0 = 1.0L, u1 = 2.0L * x;
+    for (int i = 2; i <= n; ++i) { long double u2 = 2.0L * x * u1 - u0; u0 = u1; u1 = u2; }
+    return u1;
+}
+std::vector<double> serk_coeffs(int q) {
+    const int mm = 2, s = mm * q, N = s + 1;
+    const long double mup = 19.0L / 20.0L;
+    const long double a2 = (long double)q / ((long double)s * s);
+    const long double w0 = 1.0L + mup / ((long double)s * s);
+    const long double w1 = chebT(s, w0) / ((long double)s * chebU(s - 1, w0));
+    std::vector<std::vector<long double>> A(N, std::vector<long double>(N + 1, 0.0L));
+    for (int zi = 0; zi < N; ++zi) {
+        const long double z = (long double)(zi + 1);
+        A[zi][N] = chebT(s, w0 + w1 * z) / chebT(s, w0);
+        A[zi][0] = chebT(0, 1.0L + a2 * z);
+        for (int j = 1; j <= q; ++j) {
+            const long double tmj = std::pow(chebT(mm, 1.0L + a2 * z), j - 1);
+            for (int i = 1; i <= mm; ++i) A[zi][i + mm * (j - 1)] = chebT(i, 1.0L + a2 * z) * tmj;
+        }
+    }
+    for (int i = 0; i < N; ++i) {
+        int mx = i;
+        for (int k = i + 1; k < N; ++k) if (std::fabs(A[k][i]) > std::fabs(A[mx][i])) mx = k;
+        std::swap(A[i], A[mx]);
+        for (int k = i + 1; k < N; ++k) {
+            const long double f = A[k][i] / A[i][i];
+            for (int j = i; j <= N; ++j) A[k][j] -= f * A[i][j];
+        }
+    }
+    std::vector<long double> x(N);
+    for (int i = N - 1; i >= 0; --i) {
+        x[i] = A[i][N];
+        for (int j = i + 1; j < N; ++j) x[i] -= A[i][j] * x[j];
+        x[i] /= A[i][i];
+    }
+    std::vector<double> out(N);
+    for (int i = 0; i < N; ++i) out[i] = (double)x[i];
+    return out;
+}
+
 }
 
 extern "C" {
@@ -435,26 +423,12 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     const size_t L = cfg->len, m = cfg->depth;
     if (L < 4 || L > 4096 || m < 2 || m > L) return fail(DYN_ERR_INVALID, "len must be in [4, 4096] and 2 <= depth <= len");
     if (cfg->precision != DYN_FP64 && cfg->precision != DYN_MIXED) return fail(DYN_ERR_INVALID, "unknown precision");
-    if (!tb->theta || !tb->phi2 || !tb->integ || !tb->indsA1y || !tb->indsA2y || !tb->indsB2y || !tb->weightsA1y ||
-        !tb->weightsA2y || !tb->weightsB2y)
-        return fail(DYN_ERR_INVALID, "missing table");
-    for (size_t i = 1; i < L; ++i)
-        if (!(tb->theta[i] >= tb->theta[i - 1])) return fail(DYN_ERR_INVALID, "theta must be non-decreasing");
-    if (tb->theta[0] < 0.0 || tb->theta[L - 1] != 1.0) return fail(DYN_ERR_INVALID, "theta must span [0, 1]");
     const size_t L2 = L * L;
     std::vector<int> i32[3];
-    const int64_t* src[3] = {tb->indsA1y, tb->indsA2y, tb->indsB2y};
-    for (int k = 0; k < 3; ++k) {
-        i32[k].resize(L2);
-        for (size_t e = 0; e < L2; ++e) {
-            const int64_t v = src[k][e];
-            if (v < 0 || (size_t)v + m > L) return fail(DYN_ERR_INVALID, "stencil start out of range [0, len-depth]");
-            i32[k][e] = (int)v;
-        }
+    {
+        std::string why;
+        if (!check_tables(L, m, tb, i32, why)) return fail(DYN_ERR_INVALID, why);
     }
-    for (size_t e = 0; e < L2; ++e)
-        if (!(tb->phi2[e] >= 0.0 && tb->phi2[e] <= 1.0)) return fail(DYN_ERR_INVALID, "phi2 outside [0, 1]");
-    if (tb->phi2[L2 - 1] != 1.0) return fail(DYN_ERR_INVALID, "phi2 must end at 1");
 
     Ctx* c = new Ctx();
     c->cfg = *cfg;
@@ -481,17 +455,7 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     d.tpb = d.mixed ? 128 : 64;
     d.kpt = d.mixed ? 1 : (L >= 512 ? 4 : (L >= 256 ? 2 : 1));
     d.nch = (int)((L + (size_t)d.tpb * d.kpt - 1) / ((size_t)d.tpb * d.kpt));
-    DModel& M = d.M;
-    M.p = cfg->p;
-    M.p2 = cfg->p2;
-    M.cA = cfg->lambda * cfg->p;
-    M.cB = (1 - cfg->lambda) * cfg->p2;
-    M.cC = cfg->lambda * cfg->p * (cfg->p - 1);
-    M.cD = (1 - cfg->lambda) * cfg->p2 * (cfg->p2 - 1);
-    M.cE = cfg->lambda * cfg->p * (cfg->p - 1) * (cfg->p - 2);
-    M.cF = (1 - cfg->lambda) * cfg->p2 * (cfg->p2 - 1) * (cfg->p2 - 2);
-    M.T0 = cfg->T0;
-    M.Gamma = cfg->Gamma;
+    d.M = make_model(cfg->p, cfg->p2, cfg->lambda, cfg->T0, cfg->Gamma);
 
     dyn_status s;
     const int G = (int)((L + EPI_ROWS - 1) / EPI_ROWS);

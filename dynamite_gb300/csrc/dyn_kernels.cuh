@@ -24,6 +24,8 @@ struct StageDev {
     int nb2_reuse, nb2_save; // next stage's posB2x flags (for the B2 clamp)
     int ncoef, serk_mode;    // serk_mode: 0 first stage, 1 even, 2 odd
     int maxceil, maxX;       // B1 Floor clamp and B2 row clamp of this stage (from nrows)
+    int fresh;               // 1: the gather searches the B1 positions itself (after a rollback)
+    int pad_;
     double T;        // t1grid.back() while this stage's RHS is evaluated
     double T_next;   // time of the row this stage writes
     double tdiff;    // T_next - t1grid[n0-1]
@@ -93,6 +95,23 @@ struct DevCtx {
     double* ip;            // [16][L*L]
     double* rint;          // [L]
 };
+
+// Model coefficients in the reference's host evaluation order
+// (math_ops.cpp:27-37: (lambda*p)*(p-1)... with p as the integer exponent)
+inline DModel make_model(int p, int p2, double lambda, double T0, double Gamma) {
+    DModel M;
+    M.p = p;
+    M.p2 = p2;
+    M.cA = lambda * p;
+    M.cB = (1 - lambda) * p2;
+    M.cC = lambda * p * (p - 1);
+    M.cD = (1 - lambda) * p2 * (p2 - 1);
+    M.cE = lambda * p * (p - 1) * (p - 2);
+    M.cF = (1 - lambda) * p2 * (p2 - 1) * (p2 - 2);
+    M.T0 = T0;
+    M.Gamma = Gamma;
+    return M;
+}
 
 // Launch with programmatic stream serialization (overlaps the launch with the
 // previous kernel's tail; the kernel itself calls wait_prior_grid first).

@@ -14,389 +14,20 @@
 // interval length), so interval indices equal the FP64 form's.  FP32 copies
 // of int.dat and 1/delta_t_ratio keep conversions off the (slow) FP64 pipe.
 #include <cmath>
-#include "dyn_kernels.cuh"
+#include "dyn_mixed.cuh"
 
 namespace dyn {
-
-namespace {
-
-struct FModel {
-    int p, p2;
-    float cA, cB, cC, cD;
-};
-
-template <int E>
-__device__ __forceinline__ float fpow_c(float q) {
-    if constexpr (E <= 0) return 1.0f;
-    else if constexpr (E == 1) return q;
-    else if constexpr (E == 2) return q * q;
-    else if constexpr (E == 3) return (q * q) * q;
-    else if constexpr (E == 4) { float s = q * q; return s * s; }
-    else { float s = fpow_c<E / 2>(q); s = s * s; if constexpr (E & 1) s = s * q; return s; }
-}
-__device__ __forceinline__ float fpow_r(float q, int e) {
-    float r = 1.0f, c = q;
-    while (e > 0) { if (e & 1) r *= c; c *= c; e >>= 1; }
-    return r;
-}
-
-template <int P, int P2>
-struct SigF {
-    __device__ __forceinline__ static void d12(const FModel& M, float q, float& a, float& b) {
-        if constexpr (P >= 0) {
-            a = fmaf(M.cA, fpow_c<P - 1>(q), M.cB * fpow_c<P2 - 1>(q));
-            b = fmaf(M.cC, fpow_c<P - 2>(q), M.cD * fpow_c<P2 - 2>(q));
-        } else {
-            a = fmaf(M.cA, fpow_r(q, M.p - 1), M.cB * fpow_r(q, M.p2 - 1));
-            b = fmaf(M.cC, fpow_r(q, M.p - 2), M.cD * fpow_r(q, M.p2 - 2));
-        }
-    }
-    __device__ __forceinline__ static float d2(const FModel& M, float q) {
-        if constexpr (P >= 0) return fmaf(M.cC, fpow_c<P - 2>(q), M.cD * fpow_c<P2 - 2>(q));
-        else return fmaf(M.cC, fpow_r(q, M.p - 2), M.cD * fpow_r(q, M.p2 - 2));
-    }
-};
-
-template <int M>
-__device__ __forceinline__ float2 dotf(const float* __restrict__ w, const float2* __restrict__ x, int m, bool ldg) {
-    float2 acc = make_float2(0.f, 0.f);
-    if constexpr (M > 0 && (M % 2) == 0) {
-        const float2* w2 = reinterpret_cast<const float2*>(w);
-#pragma unroll
-        for (int d = 0; d < M / 2; ++d) {
-            const float2 ww = __ldg(w2 + d);
-            const float2 xa = ldg ? __ldg(x + 2 * d) : x[2 * d];
-            const float2 xb = ldg ? __ldg(x + 2 * d + 1) : x[2 * d + 1];
-            acc.x = fmaf(ww.x, xa.x, acc.x);
-            acc.y = fmaf(ww.x, xa.y, acc.y);
-            acc.x = fmaf(ww.y, xb.x, acc.x);
-            acc.y = fmaf(ww.y, xb.y, acc.y);
-        }
-    } else {
-        for (int d = 0; d < m; ++d) {
-            const float ww = __ldg(w + d);
-            const float2 xa = ldg ? __ldg(x + d) : x[d];
-            acc.x = fmaf(ww, xa.x, acc.x);
-            acc.y = fmaf(ww, xa.y, acc.y);
-        }
-    }
-    return acc;
-}
-
-// sum_d w[d] * x[b + d] for a 10-tap row segment of float2 elements, read as
-// six 16-byte loads from the 16-byte boundary at or below b (element pairs)
-// instead of ten 8-byte loads: each vector load is one L1 wavefront per lane
-// on these scattered rows, which is what bounds this kernel.
-__device__ __forceinline__ float2 seg10(const float w[10], const float2* __restrict__ arr, size_t b) {
-    const size_t a = b & ~(size_t)1;
-    const bool sh = b & 1;
-    const float4* p = reinterpret_cast<const float4*>(arr + a);
-    float2 e[12];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const float4 v = __ldg(p + k);
-        e[2 * k] = make_float2(v.x, v.y);
-        e[2 * k + 1] = make_float2(v.z, v.w);
-    }
-    float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int d = 0; d < 10; ++d) {
-        const float2 x = sh ? e[d + 1] : e[d];
-        acc.x = fmaf(w[d], x.x, acc.x);
-        acc.y = fmaf(w[d], x.y, acc.y);
-    }
-    return acc;
-}
-
-// The same 10-tap segment from shared memory (the staged last row)
-__device__ __forceinline__ float2 seg10s(const float w[10], const float2* arr, int b) {
-    const int a = b & ~1;
-    const bool sh = b & 1;
-    const float4* p = reinterpret_cast<const float4*>(arr + a);
-    float2 e[12];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const float4 v = p[k];
-        e[2 * k] = make_float2(v.x, v.y);
-        e[2 * k + 1] = make_float2(v.z, v.w);
-    }
-    float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int d = 0; d < 10; ++d) {
-        const float2 x = sh ? e[d + 1] : e[d];
-        acc.x = fmaf(w[d], x.x, acc.x);
-        acc.y = fmaf(w[d], x.y, acc.y);
-    }
-    return acc;
-}
-
-__device__ __forceinline__ void load_w10(const float* w, float wv[10]) {
-    const float2* w2 = reinterpret_cast<const float2*>(w);
-#pragma unroll
-    for (int d = 0; d < 5; ++d) {
-        const float2 q = __ldg(w2 + d);
-        wv[2 * d] = q.x;
-        wv[2 * d + 1] = q.y;
-    }
-}
-
-// TwoSum accumulation: s + c carries the sum to about twice FP32 precision
-__device__ __forceinline__ void two_sum_add(float& s, float& c, float v) {
-    const float t = s + v;
-    const float bp = t - s;
-    c += (s - (t - bp)) + (v - bp);
-    s = t;
-}
-
-// (hi, lo) += (h2, l2) with TwoSum on the high parts
-__device__ __forceinline__ void pair_add(float& h, float& l, float h2, float l2) {
-    const float t = h + h2;
-    const float bp = t - h;
-    l = l + l2 + ((h - (t - bp)) + (h2 - bp));
-    h = t;
-}
-
-// Reduce-scatter of 8 compensated sums over a warp (as warp_reduce8, in FP32
-// pairs): lane l with (l & 3) == 0 ends with the warp total of value index
-// warp_reduce8_index(l) as hi + lo.
-__device__ __forceinline__ void warp_reduce8_pair(const float hv[8], const float lv[8], int lane, float& H, float& Lo) {
-    float wh[4], wl[4];
-    const bool b16 = lane & 16;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float sh = b16 ? hv[k] : hv[k + 4], sl = b16 ? lv[k] : lv[k + 4];
-        wh[k] = b16 ? hv[k + 4] : hv[k];
-        wl[k] = b16 ? lv[k + 4] : lv[k];
-        pair_add(wh[k], wl[k], __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
-    }
-    const bool b8 = lane & 8;
-    float xh[2], xl[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const float sh = b8 ? wh[k] : wh[k + 2], sl = b8 ? wl[k] : wl[k + 2];
-        xh[k] = b8 ? wh[k + 2] : wh[k];
-        xl[k] = b8 ? wl[k + 2] : wl[k];
-        pair_add(xh[k], xl[k], __shfl_xor_sync(0xffffffffu, sh, 8), __shfl_xor_sync(0xffffffffu, sl, 8));
-    }
-    const bool b4 = lane & 4;
-    float yh = b4 ? xh[1] : xh[0], yl = b4 ? xl[1] : xl[0];
-    pair_add(yh, yl, __shfl_xor_sync(0xffffffffu, b4 ? xh[0] : xh[1], 4),
-             __shfl_xor_sync(0xffffffffu, b4 ? xl[0] : xl[1], 4));
-    pair_add(yh, yl, __shfl_xor_sync(0xffffffffu, yh, 2), __shfl_xor_sync(0xffffffffu, yl, 2));
-    pair_add(yh, yl, __shfl_xor_sync(0xffffffffu, yh, 1), __shfl_xor_sync(0xffffffffu, yl, 1));
-    H = yh;
-    Lo = yl;
-}
-
-// Binary search of bsearchPosSorted (the same probes as pos_binary), returning
-// floor(position) as an integer and the offset from it in FP32.
-__device__ __forceinline__ void pos_split(const ListView& L, const float* __restrict__ inv_len, double El,
-                                          long long& X, float& x) {
-    int n0 = 1, n1 = L.n, m = 1;
-    double Lm = 0.0;
-    const long long kE = okey(El);
-    if (okey(L.at(0)) < kE) {
-        while (n0 <= n1) {
-            m = (n0 + n1) >> 1;
-            Lm = L.at(m - 1);
-            const long long k = okey(Lm);
-            if (k == kE) { n0 = m; break; }
-            if (k < kE) n0 = m + 1; else n1 = m - 1;
-        }
-    }
-    if (okey(Lm) <= kE) {
-        if (m == L.n) { X = m; x = 0.f; return; }
-        // interval [list[m-1], list[m]]: one FP64 difference, FP32 scale
-        const float f = (float)(El - Lm) * __ldg(inv_len + (m - 1));
-        if (f >= 1.0f) { X = m + 1; x = f - 1.0f; } else { X = m; x = f; }
-        return;
-    }
-    if (m > 1) {
-        // interval [list[m-2], list[m-1]], position m - f
-        const float f = (float)(Lm - El) * __ldg(inv_len + (m - 2));
-        if (f > 0.0f) { X = m - 1; x = 1.0f - f; } else { X = m; x = -f; }
-        return;
-    }
-    X = m;
-    x = 0.f;
-}
-
-}  // namespace
 
 template <int M, int K, int P, int P2>
 __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s) {
     wait_prior_grid();
     const StageDev& sp = c.stages[s];
-    const int L = c.L, tpb = blockDim.x, i = blockIdx.y;
-    const int nrows = sp.nrows;
-    const double t = sp.T;
-    const bool live = t > 0.0;
     extern __shared__ float2 s_lastf[];
-    __shared__ float s_c[4];
-    __shared__ int s_bi[2];
-    __shared__ double s_red[8][8];
-
-    const float2* KRl = c.KRf + (size_t)(nrows - 1) * L;
-    for (int k = threadIdx.x; k < L; k += tpb) s_lastf[k] = KRl[k];
-    if (threadIdx.x == 0) s_lastf[L] = make_float2(0.f, 0.f), s_lastf[L + 1] = make_float2(0.f, 0.f);
-    if (threadIdx.x == 0) {
-        if (live) {
-            // row constants in FP64 from the master history (as k_main)
-            const double pos = c.posB1x[i];
-            long long F = (long long)floor(pos);
-            if (F < 1) F = 1; else if (F > sp.maxceil) F = sp.maxceil;
-            const double u = (double)F - pos, u2 = u * u, u3 = u2 * u;
-            const int cubic = F < nrows - 1;
-            double c0, c1, c2, c3;
-            if (cubic) {
-                c0 = 1.0 - 3.0 * u2 - 2.0 * u3; c1 = 3.0 * u2 + 2.0 * u3; c2 = u + 2.0 * u2 + u3;
-                c3 = (u2 + u3) * c.inv_dtr[F + 1];
-            } else {
-                c0 = 1.0 - u2; c1 = u2; c2 = u + u2; c3 = 0.0;
-            }
-            s_c[0] = (float)c0; s_c[1] = (float)c1; s_c[2] = (float)c2; s_c[3] = (float)c3;
-            s_bi[0] = (int)F; s_bi[1] = cubic;
-            if (blockIdx.x == 0) {
-                const double2 x0 = c.KR[(size_t)(F - 1) * L], x1 = c.KR[(size_t)F * L];
-                const double2 d1 = c.dKR[(size_t)F * L];
-                double qb = c0 * x0.x + c1 * x1.x - c2 * d1.x;
-                double ri = c0 * c.rvec[F - 1] + c1 * c.rvec[F] - c2 * c.drvec[F];
-                if (cubic) {
-                    qb -= c3 * c.dKR[(size_t)(F + 1) * L].x;
-                    ri -= c3 * c.drvec[F + 1];
-                }
-                c.rowval[i] = make_double2(qb, ri);
-            }
-        } else {
-            s_bi[0] = 1; s_bi[1] = 0;
-            s_c[0] = s_c[1] = s_c[2] = s_c[3] = 0.f;
-            if (blockIdx.x == 0) c.rowval[i] = make_double2(c.KR[0].x, c.rvec[0]);
-        }
-        if (i == 0 && blockIdx.x == 0) c.slots->q0 = c.KR[(size_t)(nrows - 1) * L].x;
-    }
-    if (threadIdx.x == 32 && blockIdx.x == 0 && sp.kind != KIND_RHS && sp.pos_reuse < 0) {
-        // next stage's B1 position of this row (see next_position in dyn_kernels.cu)
-        const ListView lvn{c.t1grid, sp.nrows_next, sp.T_next};
-        c.posB1x_next[i] = search_pos(c.search, lvn, __dmul_rn(c.theta[i], sp.T_next));
-    }
+    __shared__ mixed::RowShared sh;
+    const int i = blockIdx.y;
+    mixed::row_setup(c, sp, i, blockIdx.x == 0, s_lastf, sh);
     __syncthreads();
-
-    const FModel Mf{c.M.p, c.M.p2, (float)c.M.cA, (float)c.M.cB, (float)c.M.cC, (float)c.M.cD};
-    const int m = M > 0 ? M : c.m;
-    const float bc0 = s_c[0], bc1 = s_c[1], bc2 = s_c[2], bc3 = s_c[3];
-    const int F = s_bi[0], cubic1 = s_bi[1];
-    const int maxX = sp.maxX;
-    const float2 fill = c.KRf[0];
-    const ListView lv{c.t1grid, nrows, t};
-
-    float acc[8], cmp[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) { acc[k] = 0.f; cmp[k] = 0.f; }
-
-#pragma unroll
-    for (int kk = 0; kk < K; ++kk) {
-        const int j = blockIdx.x * tpb * K + kk * tpb + threadIdx.x;
-        if (j < L) {
-            const size_t ij = (size_t)i * L + j;
-            float2 a1, a2, b1, b2;
-            if (live) {
-                if constexpr (M == 10) {
-                    float wv[10];
-                    load_w10(c.wA1f + ij * 10, wv);
-                    a1 = seg10s(wv, s_lastf, __ldg(c.iA1 + ij));
-                    load_w10(c.wA2f + ij * 10, wv);
-                    a2 = seg10s(wv, s_lastf, __ldg(c.iA2 + ij));
-                } else {
-                    a1 = dotf<M>(c.wA1f + ij * m, s_lastf + __ldg(c.iA1 + ij), m, false);
-                    a2 = dotf<M>(c.wA2f + ij * m, s_lastf + __ldg(c.iA2 + ij), m, false);
-                }
-                {
-                    const float2 x0 = __ldg(c.KRf + (size_t)(F - 1) * L + j);
-                    const float2 x1 = __ldg(c.KRf + (size_t)F * L + j);
-                    const float2 d1 = __ldg(c.dKRf + (size_t)F * L + j);
-                    b1.x = bc0 * x0.x + bc1 * x1.x - bc2 * d1.x;
-                    b1.y = bc0 * x0.y + bc1 * x1.y - bc2 * d1.y;
-                    if (cubic1) {
-                        const float2 d2 = __ldg(c.dKRf + (size_t)(F + 1) * L + j);
-                        b1.x -= bc3 * d2.x;
-                        b1.y -= bc3 * d2.y;
-                    }
-                }
-                {
-                    long long X;
-                    float x;
-                    pos_split(lv, c.inv_len_f, __dmul_rn(__ldg(c.phi2 + ij), t), X, x);
-                    if (X > maxX) { x += (float)(X - maxX); X = maxX; }
-                    if (X < 1) { x -= (float)(1 - X); X = 1; }
-                    const float x2 = x * x, x3 = x2 * x;
-                    const size_t base = (size_t)(X - 1) * L + __ldg(c.iB2 + ij);
-                    const float* w = c.wB2f + ij * m;
-                    float2 S0, S1, D1, D2 = make_float2(0.f, 0.f);
-                    const bool cubic2 = X < nrows - 1;
-                    if constexpr (M == 10) {
-                        float wv[10];
-                        const float2* w2 = reinterpret_cast<const float2*>(w);
-#pragma unroll
-                        for (int d = 0; d < 5; ++d) {
-                            const float2 q = __ldg(w2 + d);
-                            wv[2 * d] = q.x;
-                            wv[2 * d + 1] = q.y;
-                        }
-                        S0 = seg10(wv, c.KRf, base);
-                        S1 = seg10(wv, c.KRf, base + L);
-                        D1 = seg10(wv, c.dKRf, base + L);
-                        if (cubic2) D2 = seg10(wv, c.dKRf, base + 2 * L);
-                    } else {
-                        S0 = dotf<M>(w, c.KRf + base, m, true);
-                        S1 = dotf<M>(w, c.KRf + base + L, m, true);
-                        D1 = dotf<M>(w, c.dKRf + base + L, m, true);
-                        if (cubic2) D2 = dotf<M>(w, c.dKRf + base + 2 * L, m, true);
-                    }
-                    if (cubic2) {
-                        const float e0 = 1.f - 3.f * x2 + 2.f * x3, e1 = x - 2.f * x2 + x3;
-                        const float e2 = 3.f * x2 - 2.f * x3;
-                        const float e3 = (x3 - x2) * __ldg(c.inv_dtr_f + X + 1);
-                        b2.x = e0 * S0.x + e1 * D1.x + e2 * S1.x + e3 * D2.x;
-                        b2.y = e0 * S0.y + e1 * D1.y + e2 * S1.y + e3 * D2.y;
-                    } else {
-                        const float e0 = 1.f - x2, e2 = x - x2;
-                        b2.x = e0 * S0.x + x2 * S1.x + e2 * D1.x;
-                        b2.y = e0 * S0.y + x2 * S1.y + e2 * D1.y;
-                    }
-                }
-            } else {
-                a1 = a2 = b1 = b2 = fill;
-            }
-            float sKA1, dA1, sKB1, dB1, sKB2, dB2;
-            SigF<P, P2>::d12(Mf, a1.x, sKA1, dA1);
-            const float sRA1 = dA1 * a1.y;
-            const float sRA2 = SigF<P, P2>::d2(Mf, a2.x) * a2.y;
-            SigF<P, P2>::d12(Mf, b1.x, sKB1, dB1);
-            const float sRB1 = dB1 * b1.y;
-            SigF<P, P2>::d12(Mf, b2.x, sKB2, dB2);
-            const float sRB2 = dB2 * b2.y;
-            const float wj = __ldg(c.integ_f + j);
-            const float wRA2 = wj * sRA2, wQRA2 = wj * a2.y;
-            two_sum_add(acc[0], cmp[0], wRA2 * b2.x);
-            two_sum_add(acc[1], cmp[1], (wj * sRA1) * b1.x);
-            two_sum_add(acc[2], cmp[2], (wj * sKA1) * b1.y);
-            two_sum_add(acc[3], cmp[3], wQRA2 * sKB2);
-            two_sum_add(acc[4], cmp[4], (wj * a1.y) * sKB1);
-            two_sum_add(acc[5], cmp[5], (wj * a1.x) * sRB1);
-            two_sum_add(acc[6], cmp[6], wRA2 * b2.y);
-            two_sum_add(acc[7], cmp[7], wQRA2 * sRB2);
-        }
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float H, Lo;
-    warp_reduce8_pair(acc, cmp, lane, H, Lo);
-    if ((lane & 3) == 0) s_red[warp][warp_reduce8_index(lane)] = (double)H + (double)Lo;
-    __syncthreads();
-    if (threadIdx.x < 8) {
-        double sum = 0.0;
-        for (int w = 0; w < (tpb >> 5); ++w) sum += s_red[w][threadIdx.x];
-        c.part[((size_t)i * gridDim.x + blockIdx.x) * 8 + threadIdx.x] = sum;
-    }
+    mixed::chunk<M, K, P, P2>(c, sp, i, blockIdx.x, gridDim.x, s_lastf, sh);
 }
 
 namespace {

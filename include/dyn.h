@@ -252,6 +252,88 @@ typedef struct {
 } dyn_noalloc_rhs;
 dyn_status dyn_rhs_noalloc(const dyn_noalloc_rhs* args, void* stream);
 
+/* ---------------------------------------------------- batched quenches */
+/* No counterpart in the reference, which runs one quench per process
+ * (simulation_runner.cpp:125-304).  A batch holds many quenches, each with
+ * its own model, grid (grids of one length are shared), history, step
+ * controller and stopping rule, and advances every running quench by one RK
+ * stage per "tick": one persistent gather kernel over the target rows of all
+ * quenches and one epilogue kernel over their history rows, with the step
+ * planner and the controller of dyn_run (its gpu_rollback option included)
+ * running on the device, ticks replayed from a CUDA graph.  Arithmetic: the
+ * mixed form (DYN_MIXED) of a single context, stage for stage. */
+typedef struct {
+    size_t len, depth;
+    dyn_tables tables;       /* host pointers, copied at creation */
+} dyn_batch_grid;
+
+typedef struct {
+    int grid;                /* index into the grids array */
+    int p, p2;
+    double lambda, T0, Gamma;
+    double delta_t_min, delta_max;
+    double delta_t;          /* first step size (<= 0: delta_t_min) */
+    double t_stop;           /* stop once t1grid.back() >= t_stop (<= 0: no limit) */
+    long long max_steps;     /* stop after this many steps (<= 0: no limit) */
+    size_t capacity;         /* history rows held on the device (0: 4096) */
+} dyn_batch_quench;
+
+typedef struct {
+    int device;
+    void* stream;            /* cudaStream_t; NULL: the batch creates one */
+    int search;              /* DYN_SEARCH_* */
+    int gpu_rollback;        /* 1: roll back 10 rows on delta > 2 delta_max, as dyn_run */
+    int ticks_per_launch;    /* ticks per graph replay (0: 32) */
+    int threads;             /* gather CTA threads: 128 or 256 (0: 128) */
+    int targets;             /* targets per thread: 1 or 2 (0: 1) */
+    int ctas_per_sm;         /* persistent gather CTAs per SM (0: occupancy limit) */
+} dyn_batch_config;
+
+/* Quench status */
+enum {
+    DYN_QUENCH_RUNNING = 0,
+    DYN_QUENCH_DONE = 1,      /* reached t_stop */
+    DYN_QUENCH_MAXSTEPS = 2,  /* took max_steps steps */
+    DYN_QUENCH_FULL = 3       /* history capacity reached */
+};
+
+typedef struct {
+    int status;
+    int method;              /* method of the next step */
+    int loop;
+    int pad;
+    long long steps;         /* steps taken since creation / the last upload */
+    size_t n;                /* history rows */
+    double t;                /* t1grid.back() */
+    double delta_t;          /* step size of the next step */
+    double delta, delta_old;
+    double energy, r, qk0;   /* of the last step (as dyn_step_result) */
+} dyn_batch_info;
+
+/* Quenches start from the t=0 state of dyn_state_init. */
+dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* grids, int ngrids,
+                            const dyn_batch_quench* quenches, int nquench, void** batch);
+dyn_status dyn_batch_destroy(void* batch);
+/* Replace quench q's history and controller (as dyn_state_upload +
+ * dyn_controller_set); its status returns to running, steps to 0. */
+dyn_status dyn_batch_upload(void* batch, int q, const dyn_state* st, const dyn_controller* ctl);
+dyn_status dyn_batch_download(void* batch, int q, dyn_state* st);
+dyn_status dyn_batch_get_info(void* batch, int q, dyn_batch_info* info);
+/* New stopping rule for quench q; a stopped quench that the new rule allows
+ * to continue runs again. */
+dyn_status dyn_batch_set_limits(void* batch, int q, double t_stop, long long max_steps);
+/* Advance until no quench runs or max_ticks ticks have run; *ticks_out =
+ * ticks run.  Synchronous. */
+dyn_status dyn_batch_run(void* batch, long long max_ticks, long long* ticks_out);
+/* Autotuner: times the gather kernel over the current states for every
+ * tile shape (threads x targets x CTAs per SM), keeps the fastest and
+ * returns it.  Changes the order of the partial sums (the results move at
+ * the FP32-compensated level), not the algorithm. */
+dyn_status dyn_batch_tune(void* batch, int reps, int* threads, int* targets, int* ctas_per_sm, float* ms_best);
+/* Average device time of the gather kernel over `reps` launches for the
+ * current stage of every running quench (the kernel is idempotent). */
+dyn_status dyn_batch_profile(void* batch, int reps, float* ms_gather);
+
 /* ------------------------------------------------------------ tables */
 /* `RG-Evo grid -L len -M Tmax -s spline_order -m poly -o interp_order
  * -a alpha -D delta` (grid_cli.cpp:35-258) without the files: fills the
