@@ -1,18 +1,24 @@
 #!/usr/bin/env python
 """RK steps/s of the DYNAMITE per-step hot path on GB300.
 
-Workload (the plain FP64 form at L=512): mixed p-spin f(q)=(1-lam)q^3+lam q^4
-with lam=0.5 (-p 3 -q 4 -l 0.5), quench from infinite temperature to
-Gamma=0.6, poly-9 stencil tables (Tmax=1e5, spline order 5, alpha=delta=0)
-generated in-process.  The run starts at t=0, advances `--setup` controller
-iterations untimed (history grows to ~setup rows), then times `--steps`
-controller iterations (one RK step each, adaptive step size, RK54 /
-SSPRK(10,4) as the reference's controller chooses).
+Headline (`value`): the mixed-precision batched form at L=512 -- 64 quenches
+of the mixed p-spin model f(q)=(1-lam)q^3+lam q^4 (-p 3 -q 4) with
+temperatures uniform on [0.4, 1.0] and lam cycling through 0.3/0.5/0.7, from
+infinite temperature, on one poly-9 grid (Tmax=1e5, spline order 5,
+alpha=delta=0) generated in-process.  Every quench first takes `--setup`
+controller iterations untimed (history ~setup rows); then `--steps` ticks are
+timed, a tick being one RK stage of every running quench (RK54 / SSPRK(10,4)
+as each quench's controller chooses); value = RK steps completed / time.
+
+Beside it, on the same grid: the plain FP64 form of one quench (lam=0.5,
+T=0.6) after the same setup, its stage kernels and FP64 roofline; the
+single-quench mixed form on that state; the reference CPU path (oracle/
+restatement) on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Multi-GPU runs are independent replicas (one quench per GPU, no collective).
-Prints one JSON line on rank 0.
+Multi-GPU runs are independent replicas (no collective).  Prints one JSON
+line on rank 0.
 """
 from __future__ import annotations
 
@@ -29,7 +35,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "RK steps/s at L=512 (plain FP64 form)"
+METRIC = "RK steps/s at L=512: mixed+batched vs plain FP64 on GB300; adjoint/forward cost"
 UNIT = "steps/s"
 L2_BYTES = 129 * 1024 * 1024
 STAGEDEV_BYTES = 640     # sizeof(StageDev) per stage, uploaded each step
@@ -45,7 +51,9 @@ def parse():
     ap.add_argument("--L", type=int, default=512)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--no-mixed", dest="mixed", action="store_false", help="skip the mixed-precision measurement")
+    ap.add_argument("--no-mixed", dest="mixed", action="store_false", help="skip the single-quench mixed measurement")
+    ap.add_argument("--quenches", type=int, default=64)
+    ap.add_argument("--tune", action="store_true", help="autotune the batched gather tile before timing")
     return ap.parse_args()
 
 
@@ -108,9 +116,9 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def read_profile_traffic():
-    """DRAM bytes per k_main launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "k_main_fp64_L512.txt")
+def read_profile_traffic(name: str):
+    """DRAM bytes per unit from a committed ncu summary (`traffic_bytes_per_launch:` line), if any."""
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -174,7 +182,7 @@ def run_reference(args):
         impl = O.Port(og, O.Model(**model_kw()), search_mode=0, threads=0)
     cores = os.cpu_count()
     impl.init_state()
-    setup = min(args.setup, 30)
+    setup = min(args.setup, 300)
     impl.run(setup)
     for _ in range(min(args.warmup, 3)):
         impl.run(1)
@@ -189,13 +197,86 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
         "warmup": min(args.warmup, 3), "ms_per_step": 1e3 * el / k, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"mixed p-spin lam=0.5 T=0.6 quench, L={args.L}, poly-9 grid, "
-                                f"{setup} setup steps from t=0", "L": args.L},
+        "config": {"workload": f"{args.quenches} quenches at L={args.L} (mixed p-spin -p 3 -q 4, T on [0.4, 1.0], "
+                               f"lam 0.3/0.5/0.7, poly-9 grid Tmax 1e5), run one after another on the host "
+                               f"cores; sampled on the lam=0.5, T=0.6 quench", "L": args.L, "quenches": args.quenches},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": f"{k} controller iterations after {setup} setup steps"},
+                         "sample": f"{k} controller iterations of one quench after {setup} setup steps from t=0 "
+                                   f"(per-step cost does not depend on T or lam)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
+
+
+def _stages(m: int) -> int:
+    return 7 if m == 1 else (10 if m == 2 else 4 * (m - 2))
+
+
+def _batch_quenches(D, n: int, max_steps: int, capacity: int):
+    """n quenches on one L=512 grid: temperatures uniform on [0.4, 1.0], lambda cycling 0.3/0.5/0.7."""
+    return [D.Quench(grid=0, p=3, p2=4, lam=(0.3, 0.5, 0.7)[b % 3], Gamma=0.4 + 0.6 * b / max(n - 1, 1),
+                     max_steps=max_steps, capacity=capacity) for b in range(n)]
+
+
+def _fp64_single(D, torch, args, grid, dev, stream, flush, cap):
+    """Plain FP64 form, one quench: device-timed steps (L2 flushed before each), its
+    stage kernels and the state the CPU baseline starts from."""
+    sim = D.Simulation(grid, D.Model(**model_kw()), device=dev, use_graph=True, history_capacity=cap,
+                       stream=stream.cuda_stream)
+    sim.init()
+    sim.run(args.setup)
+    st = sim.download()
+    c = sim.controller
+    cpu_state = {"state": (st.t1grid, st.dtr, st.QK, st.QR, st.dQK, st.dQR, st.rvec, st.drvec),
+                 "dt": c["delta_t"], "method": c["method"], "delta": c["delta"], "delta_old": c["delta_old"],
+                 "loop": c["loop"]}
+    sim.run(args.warmup)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ev[k][0].record(stream)
+        sim.run(1)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    ms_main, ms_epi = sim.profile_stage(reps=20)
+    out = {"value": args.steps / t, "unit": UNIT, "ms_per_step": 1e3 * t / args.steps, "history_rows": sim.n,
+           "stage_ms": {"main": ms_main, "epilogue": ms_epi}}
+    st1, c1 = sim.download(), sim.controller
+    sim.close()
+    return out, cpu_state, (st1, c1)
+
+
+def _mixed_single(D, torch, args, grid, dev, stream, flush, cap, start):
+    st0, c0 = start
+    msim = D.Simulation(grid, D.Model(**model_kw()), precision="mixed", device=dev, use_graph=True,
+                        history_capacity=cap, stream=stream.cuda_stream)
+    msim.upload(st0)
+    msim.set_controller(c0["delta_t"], c0["method"], c0["delta"], c0["delta_old"], c0["loop"])
+    msim.run(args.warmup)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ev[k][0].record(stream)
+        msim.run(1)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    mm, me = msim.profile_stage(reps=20)
+    msim.close()
+    return {"value": args.steps / t, "unit": UNIT, "ms_per_step": 1e3 * t / args.steps,
+            "stage_ms": {"main": mm, "epilogue": me}}
+
+
+def _batch_alg_bytes(L: int, m: int, n: float) -> float:
+    """Algorithmic HBM bytes of one quench-stage of the mixed gather: FP32 weights and int32
+    starts of the three stencil families, phi2 (FP64), the FP32 history rows (QK,QR) and
+    (dQK,dQR) the B1/B2 gathers touch, O(L) row data."""
+    return 3 * L * L * (4 * m + 4) + 8 * L * L + 16 * L * n + 64 * L
 
 
 def run_ours(args):
@@ -205,151 +286,126 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo", init_method="env://")
-    from dynamite_gb300 import build as B
-    B.build()
+    from dynamite_gb300 import build as Bld
+    Bld.build()
     import dynamite_gb300 as D
     from dynamite_gb300.simulation import probe_fp64
 
     dev = local
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
     grid = D.grid.generate(args.L)
     cap = args.setup + args.warmup + 2 * args.steps + 64
-    sim = D.Simulation(grid, D.Model(**model_kw()), device=dev, use_graph=True, history_capacity=cap,
-                       stream=stream.cuda_stream)
-    sim.init()
-    sim.run(args.setup)
-    # state for the CPU baseline (same point of the same run)
-    cpu_state = None
-    if rank == 0 and world == 1:
-        st = sim.download()
-        c = sim.controller
-        cpu_state = {"state": (st.t1grid, st.dtr, st.QK, st.QR, st.dQK, st.dQR, st.rvec, st.drvec),
-                     "dt": c["delta_t"], "method": c["method"], "delta": c["delta"], "delta_old": c["delta_old"],
-                     "loop": c["loop"]}
-    sim.run(args.warmup)
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    # ---- device-timed: state resident, L2 flushed before each step (outside the events)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    methods = []
+    def max_over_ranks(x):
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([x], dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            return float(tt[0])
+        return x
+
+    # ---- plain FP64 and single-quench mixed forms (the comparison points)
+    fp64, cpu_state, start = _fp64_single(D, torch, args, grid, dev, stream, flush, cap)
+    mixed = _mixed_single(D, torch, args, grid, dev, stream, flush, cap, start) if args.mixed else None
+
+    # ---- the headline: mixed precision, batched quenches, L=512
+    B = args.quenches
+    bcap = args.setup + args.warmup + args.steps + 64
+    bt = D.Batch([grid], _batch_quenches(D, B, args.setup, bcap), ticks_per_launch=32, device=dev,
+                 stream=stream.cuda_stream)
+    ticks_before = bt.run(10 ** 9)  # untimed: every quench takes `setup` steps from t=0
+    for q in range(B):
+        bt.set_limits(q, max_steps=10 ** 12)
+    tune = bt.tune(reps=3) if args.tune else None
+    ticks_before += bt.run(args.warmup)
+    hist = [i["n"] for i in bt.infos()]
+    steps0 = bt.total_steps()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
     with Clocks(dev) as clk:
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            ev[k][0].record(stream)
-            out = sim.run(1)
-            ev[k][1].record(stream)
-            methods.append(int(out["method"][0]))
+        e0.record(stream)
+        bt.enqueue(args.steps)
+        e1.record(stream)
         torch.cuda.synchronize()
     barrier()
-    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
-    t_dev = dev_ms / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt[0])
-    value = world * args.steps / t_dev
-    stages = [7 if m == 1 else (10 if m == 2 else 4 * (m - 2)) for m in methods]
+    bt.sync()
+    rk_steps = bt.total_steps() - steps0
+    t_batch = max_over_ranks(e0.elapsed_time(e1) / 1e3)
+    rk_steps_all = rk_steps * world
+    value = rk_steps_all / t_batch
 
-    # ---- end to end through the C ABI: host buffers, copies inside the timed region
-    qk, qr = np.empty(args.L), np.empty(args.L)
-    e2e_steps = max(20, args.steps // 4)
-    h2d = d2h = 0
-    t_e2e = 0.0
-    for k in range(e2e_steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        torch.cuda.synchronize()
-        m = sim.controller["method"]
-        t0 = time.perf_counter()
-        sim.run(1)
-        sim.last_row(qk, qr)
-        t_e2e += time.perf_counter() - t0
-        S = 7 if m == 1 else (10 if m == 2 else 4 * (m - 2))
-        h2d += S * STAGEDEV_BYTES
-        d2h += SLOTS_BYTES + 2 * args.L * 8
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_e2e], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt[0])
-    e2e_value = world * e2e_steps / t_e2e
-
-    # ---- the mixed-precision form on the same state (FP32 gathers/convolutions)
-    mixed = None
-    if args.mixed:
-        st0 = sim.download()
-        c0 = sim.controller
-        msim = D.Simulation(grid, D.Model(**model_kw()), precision="mixed", device=dev, use_graph=True,
-                            history_capacity=cap, stream=stream.cuda_stream)
-        msim.upload(st0)
-        msim.set_controller(c0["delta_t"], c0["method"], c0["delta"], c0["delta_old"], c0["loop"])
-        msim.run(args.warmup)
-        mev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        torch.cuda.synchronize()
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            mev[k][0].record(stream)
-            msim.run(1)
-            mev[k][1].record(stream)
-        torch.cuda.synchronize()
-        t_mix = sum(a.elapsed_time(b) for a, b in mev) / 1e3
-        mm, me = msim.profile_stage(reps=20)
-        mixed = {"value": args.steps / t_mix, "unit": UNIT, "ms_per_step": 1e3 * t_mix / args.steps,
-                 "stage_ms": {"main": mm, "epilogue": me},
-                 "speedup_vs_fp64": (args.steps / t_mix) / (args.steps / (dev_ms / 1e3))}
-        msim.close()
+    # ---- end to end through the C ABI: dyn_batch_run with its status reads, plus every
+    #      quench's newest row C(t, theta t), R(t, theta t) read back after each launch
+    rows = [(np.empty(args.L), np.empty(args.L)) for _ in range(B)]
+    reps = max(2, args.steps // 32)
+    s0 = bt.total_steps()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        bt.run(32)
+        for q in range(B):
+            bt.last_row(q, *rows[q])
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    e2e_steps = (bt.total_steps() - s0) * world
+    d2h_tick = (B * 112 + B * 2 * args.L * 8) / 32.0
 
     if rank != 0:
         return
-    # ---- roofline of the dominant kernel (gather + convolution), timed live
-    ms_main, ms_epi = sim.profile_stage(reps=20)
+    # ---- roofline of the dominant kernel: the batched gather, timed live on its stream
+    ms_gather = bt.profile(reps=10)
     L, m = args.L, grid.depth
-    alg_bytes = 3 * L * L * (8 * m + 4) + 8 * L * L + 8 * L + 16 * L
-    alg_flop = (24 * m + 122) * L * L
+    n_mean = float(np.mean(hist))
+    alg_bytes = B * _batch_alg_bytes(L, m, n_mean)
     peaks, src = measured_peaks()
+    achieved = alg_bytes / (ms_gather * 1e-3) / 1e9
+    traffic = read_profile_traffic("k_batch_gather_L512.txt")
     fp64_peak = probe_fp64(dev)
-    achieved_gbs = alg_bytes / (ms_main * 1e-3) / 1e9
-    achieved_fp64 = alg_flop / (ms_main * 1e-3) / 1e9
-    traffic = read_profile_traffic()
+    fp64_flop = (24 * m + 122) * L * L
+    fp64_achieved = fp64_flop / (fp64["stage_ms"]["main"] * 1e-3) / 1e9
     cpu = None
-    if cpu_state is not None:
+    if world == 1:
         v, k, el = cpu_port_steps_per_s(cpu_state, grid, args.cpu_seconds, args.steps)
         cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{k} controller iterations ({el:.1f} s) from the GPU run's state after {args.setup} steps"}
+               "sample": f"{k} controller iterations ({el:.1f} s) of one quench (lam=0.5, T=0.6) from the FP64 "
+                         f"run's state after {args.setup} steps; per-step cost does not depend on T or lam"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"mixed p-spin lam=0.5 T=0.6 quench, L={L}, poly-9 grid (Tmax 1e5), timed after "
-                               f"{args.setup} setup steps", "L": L, "history_rows": sim.n,
-                   "l2": "flushed before every timed step (256 MB write, outside the events)",
-                   "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
-                "d2h_bytes_per_step": d2h / e2e_steps},
-        "gpu_launches": int(2 * sum(stages)),
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": traffic,
-                     "kernel": "k_main (fused gather+convolution)", "ms_per_launch": ms_main,
-                     "peak_source": src},
-        "roofline_fp64": {"bound": "fp64", "achieved": achieved_fp64, "peak": fp64_peak, "unit": "GFLOP/s",
-                          "frac": achieved_fp64 / fp64_peak, "flop_per_launch": alg_flop,
-                          "peak_source": "measured (dyn_probe_fp64, same run)"},
-        "stage_ms": {"main": ms_main, "epilogue": ms_epi},
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"{B} quenches at L={L} (mixed p-spin -p 3 -q 4, T uniform on [0.4, 1.0], "
+                               f"lam cycling 0.3/0.5/0.7, poly-9 grid Tmax 1e5), mixed precision, batched; "
+                               f"timed after {args.setup} steps of every quench",
+                   "L": L, "quenches": B, "step": "one tick = one RK stage of every quench",
+                   "rk_steps_timed": rk_steps_all, "history_rows": [min(hist), max(hist)],
+                   "ticks_before_timed": ticks_before,
+                   "l2": "inputs larger than L2 (histories + tables of all quenches > 1 GB)",
+                   "tile": tune or {"threads": 128, "targets": 1},
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "speedup_vs_fp64": value / fp64["value"],
+        "fp64": dict(fp64, roofline={"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak,
+                                     "unit": "GFLOP/s", "frac": fp64_achieved / fp64_peak,
+                                     "flop_per_launch": fp64_flop, "kernel": "k_main (FP64 fused gather)",
+                                     "peak_source": "measured (dyn_probe_fp64, same run)"}),
+        "mixed_single": mixed,
+        "e2e": {"value": e2e_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": d2h_tick, "note": "per tick; dyn_batch_run of 32 ticks + newest rows"},
+        "gpu_launches": int(2 * args.steps),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None if traffic is None else traffic * B,
+                     "kernel": "k_batch_gather (all quenches, one stage)", "ms_per_launch": ms_gather,
+                     "alg_bytes_per_launch": alg_bytes, "peak_source": src},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
-        "mixed": mixed,
     }
+    bt.close()
     print(json.dumps(line))
 
 

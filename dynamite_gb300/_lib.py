@@ -162,6 +162,9 @@ def lib():
             "dyn_batch_get_info": ([vp, C.c_int, C.POINTER(BatchInfo)], C.c_int),
             "dyn_batch_set_limits": ([vp, C.c_int, C.c_double, C.c_longlong], C.c_int),
             "dyn_batch_run": ([vp, C.c_longlong, C.POINTER(C.c_longlong)], C.c_int),
+            "dyn_batch_enqueue": ([vp, C.c_longlong], C.c_int),
+            "dyn_batch_sync": ([vp], C.c_int),
+            "dyn_batch_last_row": ([vp, C.c_int, dp, dp], C.c_int),
             "dyn_batch_tune": ([vp, C.c_int, ip, ip, ip, C.POINTER(C.c_float)], C.c_int),
             "dyn_batch_profile": ([vp, C.c_int, C.POINTER(C.c_float)], C.c_int),
             "dyn_grid_generate": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,

@@ -95,6 +95,22 @@ class Batch:
         _lib.check(_lib.lib().dyn_batch_run(self._h, int(max_ticks), C.byref(t)), "dyn_batch_run")
         return int(t.value)
 
+    def enqueue(self, ticks: int) -> None:
+        """Enqueue `ticks` ticks on the batch's stream without waiting."""
+        _lib.check(_lib.lib().dyn_batch_enqueue(self._h, int(ticks)), "dyn_batch_enqueue")
+
+    def sync(self) -> None:
+        """Wait for enqueued ticks and refresh the quench infos."""
+        _lib.check(_lib.lib().dyn_batch_sync(self._h), "dyn_batch_sync")
+
+    def last_row(self, q: int, qK: np.ndarray | None = None, qR: np.ndarray | None = None):
+        """C(t, theta t) and R(t, theta t) of quench q's newest row."""
+        L = self.grids[self.quenches[q].grid].L
+        qK = np.empty(L) if qK is None else qK
+        qR = np.empty(L) if qR is None else qR
+        _lib.check(_lib.lib().dyn_batch_last_row(self._h, q, _lib.ptr(qK), _lib.ptr(qR)), "dyn_batch_last_row")
+        return qK, qR
+
     def info(self, q: int) -> dict:
         i = _lib.BatchInfo()
         _lib.check(_lib.lib().dyn_batch_get_info(self._h, q, C.byref(i)), "dyn_batch_get_info")

@@ -222,20 +222,22 @@ __device__ void finish_step(const Quench& q, Plan& pl, const StageDev& last, con
 }
 
 // ------------------------------------------------------------------ kernels
-// TPB threads per CTA; the register cap keeps eight (K = 1) or four (K = 2)
-// 128-thread CTAs' worth of threads resident per SM.
+// TPB threads per CTA; the register cap keeps 1280 (K = 1) or 512 (K = 2)
+// threads resident per SM (48 / 128 registers): the gathers are latency-bound.
 template <int M, int K, int P, int P2, int TPB>
-__global__ void __launch_bounds__(TPB, (K == 1 ? 1024 : 512) / TPB) k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL,
-                                                      const unsigned* __restrict__ items, const unsigned nitems,
-                                                      Work* work) {
+__global__ void __launch_bounds__(TPB, (K == 1 ? 1280 : 512) / TPB)
+    k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,
+                   const unsigned nitems, Work* work) {
     wait_prior_grid();
     extern __shared__ float2 s_lastf[];
     __shared__ mixed::RowShared sh;
-    __shared__ unsigned s_item;
+    __shared__ unsigned s_item[2];  // the item being worked on and the next one
+    constexpr int GMAX = mixed::RED_CAP / (8 * (TPB / 32));  // chunks per fold
+    int p = 0;
+    if (threadIdx.x == 0) s_item[0] = atomicAdd(&work->next, 1u);
+    __syncthreads();
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&work->next, 1u);
-        __syncthreads();
-        const unsigned it = s_item;
+        const unsigned it = s_item[p];
         if (it >= nitems) break;
         const unsigned e = __ldg(items + it);
         const Quench& q = Q[e >> 16];
@@ -246,12 +248,18 @@ __global__ void __launch_bounds__(TPB, (K == 1 ? 1024 : 512) / TPB) k_batch_gath
             mixed::row_setup(q.c, sp, i, true, s_lastf, sh);
             __syncthreads();
             const int nch = q.c.nch;
-            for (int ch = 0; ch < nch; ++ch) {
-                mixed::chunk<M, K, P, P2>(q.c, sp, i, ch, nch, s_lastf, sh);
+            for (int ch0 = 0; ch0 < nch; ch0 += GMAX) {
+                const int ng = min(GMAX, nch - ch0);
+                for (int g = 0; g < ng; ++g) mixed::chunk_sums<M, K, P, P2>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
                 __syncthreads();
+                mixed::fold_chunks(q.c, i, nch, ch0, ng, sh);
+                if (ch0 + GMAX < nch) __syncthreads();
             }
         }
-        __syncthreads();  // every thread has read s_item and the shared row
+        // the next item goes to the other slot: threads still reading s_item[p] are unaffected
+        if (threadIdx.x == 0) s_item[p ^ 1] = atomicAdd(&work->next, 1u);
+        __syncthreads();
+        p ^= 1;
     }
     if (threadIdx.x == 0 && atomicAdd(&work->done, 1u) == gridDim.x - 1) {
         // every CTA has made its last fetch: reset for the next launch
@@ -324,6 +332,8 @@ struct Batch {
     std::vector<Quench> qh;  // host copy: pointers and constants (pl is the device's)
     std::vector<Plan> plan_h;
     Plan* plan_pin = nullptr;
+    double2* row_pin = nullptr;
+    size_t row_pin_len = 0;
     Quench* qd = nullptr;
     Plan* pd = nullptr;
     TabDev* tabd = nullptr;
@@ -343,6 +353,7 @@ struct Batch {
         if (graph) cudaGraphExecDestroy(graph);
         for (void* p : allocs) cudaFree(p);
         if (plan_pin) cudaFreeHost(plan_pin);
+        if (row_pin) cudaFreeHost(row_pin);
         if (own_stream && st) cudaStreamDestroy(st);
     }
 
@@ -825,7 +836,8 @@ dyn_status dyn_batch_run(void* p, long long max_ticks, long long* ticks_out) {
     if (!p) return bfail(DYN_ERR_INVALID, "null argument");
     Batch* bt = BT(p);
     long long done = 0;
-    dyn_status s;
+    dyn_status s = bt->read_plans();
+    if (s) return s;
     while (done < max_ticks && bt->running() > 0) {
         if ((s = bt->ensure_graph())) return s;
         if (max_ticks - done >= bt->graph_ticks) {
@@ -838,6 +850,45 @@ dyn_status dyn_batch_run(void* p, long long max_ticks, long long* ticks_out) {
         if ((s = bt->read_plans())) return s;
     }
     if (ticks_out) *ticks_out = done;
+    return DYN_OK;
+}
+
+dyn_status dyn_batch_enqueue(void* p, long long ticks) {
+    if (!p || ticks < 0) return bfail(DYN_ERR_INVALID, "bad argument");
+    Batch* bt = BT(p);
+    dyn_status s = bt->ensure_graph();
+    if (s) return s;
+    long long done = 0;
+    for (; done + bt->graph_ticks <= ticks; done += bt->graph_ticks) BCK(cudaGraphLaunch(bt->graph, bt->st));
+    return bt->enqueue_ticks((int)(ticks - done));
+}
+
+dyn_status dyn_batch_sync(void* p) {
+    if (!p) return bfail(DYN_ERR_INVALID, "null argument");
+    return BT(p)->read_plans();
+}
+
+dyn_status dyn_batch_last_row(void* p, int qi, double* qK, double* qR) {
+    if (!p || !qK || !qR) return bfail(DYN_ERR_INVALID, "null argument");
+    Batch* bt = BT(p);
+    if (qi < 0 || qi >= (int)bt->qh.size()) return bfail(DYN_ERR_INVALID, "quench index out of range");
+    const Quench& q = bt->qh[qi];
+    const int L = q.c.L;
+    const size_t n = (size_t)bt->plan_h[qi].n;
+    if (bt->row_pin_len < (size_t)L) {
+        if (bt->row_pin) cudaFreeHost(bt->row_pin);
+        bt->row_pin = nullptr;
+        bt->row_pin_len = 0;
+        if (cudaMallocHost((void**)&bt->row_pin, L * sizeof(double2)) != cudaSuccess)
+            return bfail(DYN_ERR_NOMEM, "cudaMallocHost failed");
+        bt->row_pin_len = L;
+    }
+    BCK(cudaMemcpyAsync(bt->row_pin, q.c.KR + (n - 1) * L, L * sizeof(double2), cudaMemcpyDeviceToHost, bt->st));
+    BCK(cudaStreamSynchronize(bt->st));
+    for (int i = 0; i < L; ++i) {
+        qK[i] = bt->row_pin[i].x;
+        qR[i] = bt->row_pin[i].y;
+    }
     return DYN_OK;
 }
 

@@ -18,8 +18,9 @@
 
 namespace dyn {
 
+// 128 threads; the register cap (48 at one target per thread) keeps ten CTAs per SM
 template <int M, int K, int P, int P2>
-__global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s) {
+__global__ void __launch_bounds__(128, K == 1 ? 10 : 4) k_main_mixed(const DevCtx c, const int s) {
     wait_prior_grid();
     const StageDev& sp = c.stages[s];
     extern __shared__ float2 s_lastf[];
@@ -27,7 +28,9 @@ __global__ void __launch_bounds__(128) k_main_mixed(const DevCtx c, const int s)
     const int i = blockIdx.y;
     mixed::row_setup(c, sp, i, blockIdx.x == 0, s_lastf, sh);
     __syncthreads();
-    mixed::chunk<M, K, P, P2>(c, sp, i, blockIdx.x, gridDim.x, s_lastf, sh);
+    mixed::chunk_sums<M, K, P, P2>(c, sp, blockIdx.x, 0, s_lastf, sh, i);
+    __syncthreads();
+    mixed::fold_chunks(c, i, gridDim.x, blockIdx.x, 1, sh);
 }
 
 namespace {

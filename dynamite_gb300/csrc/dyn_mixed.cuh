@@ -211,10 +211,11 @@ __device__ __forceinline__ void pos_split(const ListView& L, const float* __rest
 
 
 // Block-shared scratch of one target row
+constexpr int RED_CAP = 512;  // per-warp partial sums held between folds (doubles)
 struct RowShared {
-    float c[4];      // B1 Hermite constants of the row (FP32)
-    int bi[2];       // B1 floor index, cubic flag
-    double red[8][8];  // per-warp partial sums (up to 8 warps)
+    float c[4];            // B1 Hermite constants of the row (FP32)
+    int bi[2];             // B1 floor index, cubic flag
+    double red[RED_CAP];   // [chunk slot][warp][8] partial sums
 };
 
 // Row set-up for target row i: stages the last history row (FP32 mirror) in
@@ -277,13 +278,12 @@ __device__ __forceinline__ void row_setup(const DevCtx& c, const StageDev& sp, c
 
 // One chunk of tpb*K targets of row i: A1/A2 from the staged row, B1 and B2
 // from the FP32 history, Sigma, and the eight int.dat-weighted products with
-// TwoSum accumulation; the block's eight sums land in part[i][ch][0..8).
-// Call after row_setup and a __syncthreads(); ends after a __syncthreads()
-// that makes sh.red readable, so callers that loop must sync again before
-// the next chunk writes sh.red.
+// TwoSum accumulation; each warp's eight sums land in sh.red[slot][warp].
+// Call after row_setup and a __syncthreads(); no barrier inside, so a block
+// can run several chunks (slots) before one fold.
 template <int M, int K, int P, int P2>
-__device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const int i, const int ch, const int nch,
-                                      const float2* s_lastf, RowShared& sh) {
+__device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, const int ch, const int slot,
+                                           const float2* s_lastf, RowShared& sh, const int i) {
     const int L = c.L, tpb = blockDim.x;
     const int nrows = sp.nrows;
     const double t = sp.T;
@@ -391,12 +391,20 @@ __device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float H, Lo;
     warp_reduce8_pair(acc, cmp, lane, H, Lo);
-    if ((lane & 3) == 0) sh.red[warp][warp_reduce8_index(lane)] = (double)H + (double)Lo;
-    __syncthreads();
-    if (threadIdx.x < 8) {
+    if ((lane & 3) == 0) sh.red[((slot * (tpb >> 5)) + warp) * 8 + warp_reduce8_index(lane)] = (double)H + (double)Lo;
+}
+
+// After a __syncthreads() that follows chunk_sums of slots 0..ng-1 (chunks
+// ch0..ch0+ng-1): the block sums of each chunk, warps added in order, into
+// part[i][ch][0..8).
+__device__ __forceinline__ void fold_chunks(const DevCtx& c, const int i, const int nch, const int ch0, const int ng,
+                                            const RowShared& sh) {
+    const int nw = blockDim.x >> 5;
+    for (int t = threadIdx.x; t < 8 * ng; t += blockDim.x) {
+        const int g = t >> 3, k = t & 7;
         double sum = 0.0;
-        for (int w = 0; w < (tpb >> 5); ++w) sum += sh.red[w][threadIdx.x];
-        c.part[((size_t)i * nch + ch) * 8 + threadIdx.x] = sum;
+        for (int w = 0; w < nw; ++w) sum += sh.red[(g * nw + w) * 8 + k];
+        c.part[((size_t)i * nch + ch0 + g) * 8 + k] = sum;
     }
 }
 

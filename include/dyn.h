@@ -318,6 +318,7 @@ dyn_status dyn_batch_destroy(void* batch);
  * dyn_controller_set); its status returns to running, steps to 0. */
 dyn_status dyn_batch_upload(void* batch, int q, const dyn_state* st, const dyn_controller* ctl);
 dyn_status dyn_batch_download(void* batch, int q, dyn_state* st);
+/* Quench q's status and controller as of the last run/sync/upload. */
 dyn_status dyn_batch_get_info(void* batch, int q, dyn_batch_info* info);
 /* New stopping rule for quench q; a stopped quench that the new rule allows
  * to continue runs again. */
@@ -325,6 +326,14 @@ dyn_status dyn_batch_set_limits(void* batch, int q, double t_stop, long long max
 /* Advance until no quench runs or max_ticks ticks have run; *ticks_out =
  * ticks run.  Synchronous. */
 dyn_status dyn_batch_run(void* batch, long long max_ticks, long long* ticks_out);
+/* Enqueue `ticks` ticks on the batch's stream and return (stopped quenches
+ * skip them); dyn_batch_sync waits and refreshes what dyn_batch_get_info
+ * reports. */
+dyn_status dyn_batch_enqueue(void* batch, long long ticks);
+dyn_status dyn_batch_sync(void* batch);
+/* Quench q's newest history row C(t, theta_j t), R(t, theta_j t) (as of the
+ * last run/sync) into host buffers of its grid length. */
+dyn_status dyn_batch_last_row(void* batch, int q, double* qK, double* qR);
 /* Autotuner: times the gather kernel over the current states for every
  * tile shape (threads x targets x CTAs per SM), keeps the fastest and
  * returns it.  Changes the order of the partial sums (the results move at
