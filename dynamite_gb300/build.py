@@ -54,7 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cu, cxx = _sources()
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(INCLUDE, "dyn.h")]
     stamp = os.path.join(OUT, "stamp")
-    dig = _digest(deps) + os.uname().machine
+    extra = os.environ.get("DYN_NVCC_EXTRA", "").split()  # e.g. -DDYN_BATCH_TPSM=1152 for tuning builds
+    dig = _digest(deps) + os.uname().machine + " ".join(extra)
     if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == dig:
         return LIB
     # host code: IEEE arithmetic as written (no FMA contraction on any host ISA), so the
@@ -64,7 +65,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     jobs = []
     for s in cu:
         obj = os.path.join(OUT, s + ".o")
-        jobs.append([nvcc, *ARCH, "-lineinfo", *common, "-c", os.path.join(SRC, s), "-o", obj])
+        jobs.append([nvcc, *ARCH, "-lineinfo", *common, *extra, "-c", os.path.join(SRC, s), "-o", obj])
     for s in cxx:
         obj = os.path.join(OUT, s + ".o")
         jobs.append([nvcc, *common, "-x", "c++", "-c", os.path.join(SRC, s), "-o", obj])

@@ -488,15 +488,17 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
 #undef UP
     cudaMemset(d.slots, 0, sizeof(Slots));
     if (d.mixed) {
-        float *f1, *f2, *f3;
-        if ((s = dalloc(&f1, L2 * m)) || (s = dalloc(&f2, L2 * m)) || (s = dalloc(&f3, L2 * m))) { delete c; return s; }
+        const size_t planes = (m + 1) / 2;
+        float2 *f1, *f2, *f3;
+        if ((s = dalloc(&f1, planes * L2)) || (s = dalloc(&f2, planes * L2)) || (s = dalloc(&f3, planes * L2))) { delete c; return s; }
         d.wA1f = f1; d.wA2f = f2; d.wB2f = f3;
         float* itf;
         if ((s = dalloc(&itf, L))) { delete c; return s; }
         d.integ_f = itf;
         if (launch_weights_f32(it, itf, L, c->st) != cudaSuccess) { delete c; return fail(DYN_ERR_CUDA, "FP32 int.dat copy failed"); }
-        if (launch_weights_f32(w1, f1, L2 * m, c->st) != cudaSuccess || launch_weights_f32(w2, f2, L2 * m, c->st) != cudaSuccess ||
-            launch_weights_f32(w3, f3, L2 * m, c->st) != cudaSuccess || cudaStreamSynchronize(c->st) != cudaSuccess) {
+        if (launch_weights_tapmajor(w1, f1, L2, (int)m, c->st) != cudaSuccess ||
+            launch_weights_tapmajor(w2, f2, L2, (int)m, c->st) != cudaSuccess ||
+            launch_weights_tapmajor(w3, f3, L2, (int)m, c->st) != cudaSuccess || cudaStreamSynchronize(c->st) != cudaSuccess) {
             delete c;
             return fail(DYN_ERR_CUDA, "FP32 weight copies failed");
         }

@@ -222,10 +222,13 @@ __device__ void finish_step(const Quench& q, Plan& pl, const StageDev& last, con
 }
 
 // ------------------------------------------------------------------ kernels
-// TPB threads per CTA; the register cap keeps 1280 (K = 1) or 512 (K = 2)
-// threads resident per SM (48 / 128 registers): the gathers are latency-bound.
+// TPB threads per CTA; the register cap keeps DYN_BATCH_TPSM (K = 1) or 512
+// (K = 2) threads resident per SM: the gathers are latency-bound.
+#ifndef DYN_BATCH_TPSM
+#define DYN_BATCH_TPSM 1280
+#endif
 template <int M, int K, int P, int P2, int TPB>
-__global__ void __launch_bounds__(TPB, (K == 1 ? 1280 : 512) / TPB)
+__global__ void __launch_bounds__(TPB, (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
     k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,
                    const unsigned nitems, Work* work) {
     wait_prior_grid();
@@ -319,7 +322,7 @@ struct GridDev {
     double* integ = nullptr;
     float* integ_f = nullptr;
     int* iA[3] = {nullptr, nullptr, nullptr};
-    float* wf[3] = {nullptr, nullptr, nullptr};
+    float2* wf[3] = {nullptr, nullptr, nullptr};  // tap-major FP32 pair planes
 };
 
 struct Batch {
@@ -563,7 +566,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         const dyn_tables& tb = grids[g].tables;
         if ((s = bt->alloc(&gd.theta, L)) || (s = bt->alloc(&gd.phi2, L2)) || (s = bt->alloc(&gd.integ, L)) ||
             (s = bt->alloc(&gd.integ_f, L))) { delete bt; return s; }
-        std::vector<float> f(L2 * m);
+        std::vector<float> f(L);
         for (size_t k = 0; k < L; ++k) f[k] = (float)tb.integ[k];
 #define BUP(dst, src, bytes)                                                                       \
     if ((e = cudaMemcpy((void*)(dst), (src), (bytes), cudaMemcpyHostToDevice)) != cudaSuccess) {  \
@@ -575,11 +578,16 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         BUP(gd.integ, tb.integ, L * sizeof(double));
         BUP(gd.integ_f, f.data(), L * sizeof(float));
         const double* w[3] = {tb.weightsA1y, tb.weightsA2y, tb.weightsB2y};
+        const size_t planes = (m + 1) / 2;
+        std::vector<float2> wt(planes * L2);
         for (int k = 0; k < 3; ++k) {
-            if ((s = bt->alloc(&gd.iA[k], L2)) || (s = bt->alloc(&gd.wf[k], L2 * m))) { delete bt; return s; }
+            if ((s = bt->alloc(&gd.iA[k], L2)) || (s = bt->alloc(&gd.wf[k], planes * L2))) { delete bt; return s; }
             BUP(gd.iA[k], i32[k].data(), L2 * sizeof(int));
-            for (size_t x = 0; x < L2 * m; ++x) f[x] = (float)w[k][x];
-            BUP(gd.wf[k], f.data(), L2 * m * sizeof(float));
+            // the layout of k_weights_tapmajor (dyn_mixed.cu)
+            for (size_t e = 0; e < L2; ++e)
+                for (size_t d = 0; d < m; d += 2)
+                    wt[(d >> 1) * L2 + e] = make_float2((float)w[k][e * m + d], d + 1 < m ? (float)w[k][e * m + d + 1] : 0.0f);
+            BUP(gd.wf[k], wt.data(), planes * L2 * sizeof(float2));
         }
     }
     bt->M = all10 ? 10 : 0;

@@ -82,10 +82,11 @@ struct DevCtx {
     Slots* slots;
     StageDev* stages;      // [SMAX]
     double2* rhs_out;      // [L]
-    // mixed form: FP32 copies of the weights and FP32 mirror of the history
-    const float* wA1f;
-    const float* wA2f;
-    const float* wB2f;
+    // mixed form: FP32 copies of the weights, tap-major ([ceil(m/2)][L*L] tap
+    // pairs), and FP32 mirror of the history
+    const float2* wA1f;
+    const float2* wA2f;
+    const float2* wB2f;
     float2* KRf;
     float2* dKRf;
     const float* integ_f;  // [L]   int.dat in FP32
@@ -158,6 +159,8 @@ cudaError_t launch_pack_rows(const double* QK, const double* QR, double2* out, s
 cudaError_t launch_main_mixed(const DevCtx& c, int s, cudaStream_t st);
 cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cudaStream_t st);
 cudaError_t launch_weights_f32(const double* in, float* out, size_t count, cudaStream_t st);
+// [L*L][m] FP64 stencil rows to the tap-major FP32 pair planes of the mixed form
+cudaError_t launch_weights_tapmajor(const double* in, float2* out, size_t targets, int m, cudaStream_t st);
 cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr,
                             cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);

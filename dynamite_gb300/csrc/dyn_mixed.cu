@@ -75,6 +75,14 @@ __global__ void k_weights_f32(const double* in, float* out, size_t count) {
         out[e] = (float)in[e];
 }
 
+// out[p][e] = (w[e][2p], w[e][2p+1]) in FP32 (second tap 0 past the depth)
+__global__ void k_weights_tapmajor(const double* in, float2* out, size_t targets, int m) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < targets; e += (size_t)gridDim.x * blockDim.x)
+        for (int d = 0; d < m; d += 2)
+            out[(size_t)(d >> 1) * targets + e] =
+                make_float2((float)in[e * m + d], d + 1 < m ? (float)in[e * m + d + 1] : 0.0f);
+}
+
 }  // namespace
 
 cudaError_t launch_main_mixed(const DevCtx& c, int s, cudaStream_t st) {
@@ -92,6 +100,12 @@ cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cud
 cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr,
                             cudaStream_t st) {
     k_time_f32<<<(n + 255) / 256, 256, 0, st>>>(t1, dtr, n, inv_len, inv_dtr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weights_tapmajor(const double* in, float2* out, size_t targets, int m, cudaStream_t st) {
+    const int blocks = (int)((targets + 255) / 256 < 8192 ? (targets + 255) / 256 : 8192);
+    k_weights_tapmajor<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, targets, m);
     return cudaGetLastError();
 }
 

@@ -45,27 +45,22 @@ struct SigF {
     }
 };
 
-template <int M>
-__device__ __forceinline__ float2 dotf(const float* __restrict__ w, const float2* __restrict__ x, int m, bool ldg) {
+// FP32 stencil weights are tap-major: plane p holds the tap pair (2p, 2p+1)
+// of every target (float2, the second tap zero for an odd depth), so the
+// lanes of a warp, handling consecutive targets, read consecutive words.
+// sum_d w[d] * x[d] over the m taps of target ij, taps in order.
+__device__ __forceinline__ float2 dotfT(const float2* __restrict__ w, size_t L2, size_t ij,
+                                        const float2* __restrict__ x, int m, bool ldg) {
     float2 acc = make_float2(0.f, 0.f);
-    if constexpr (M > 0 && (M % 2) == 0) {
-        const float2* w2 = reinterpret_cast<const float2*>(w);
-#pragma unroll
-        for (int d = 0; d < M / 2; ++d) {
-            const float2 ww = __ldg(w2 + d);
-            const float2 xa = ldg ? __ldg(x + 2 * d) : x[2 * d];
-            const float2 xb = ldg ? __ldg(x + 2 * d + 1) : x[2 * d + 1];
-            acc.x = fmaf(ww.x, xa.x, acc.x);
-            acc.y = fmaf(ww.x, xa.y, acc.y);
+    for (int d = 0; d < m; d += 2) {
+        const float2 ww = __ldg(w + (size_t)(d >> 1) * L2 + ij);
+        const float2 xa = ldg ? __ldg(x + d) : x[d];
+        acc.x = fmaf(ww.x, xa.x, acc.x);
+        acc.y = fmaf(ww.x, xa.y, acc.y);
+        if (d + 1 < m) {
+            const float2 xb = ldg ? __ldg(x + d + 1) : x[d + 1];
             acc.x = fmaf(ww.y, xb.x, acc.x);
             acc.y = fmaf(ww.y, xb.y, acc.y);
-        }
-    } else {
-        for (int d = 0; d < m; ++d) {
-            const float ww = __ldg(w + d);
-            const float2 xa = ldg ? __ldg(x + d) : x[d];
-            acc.x = fmaf(ww, xa.x, acc.x);
-            acc.y = fmaf(ww, xa.y, acc.y);
         }
     }
     return acc;
@@ -118,11 +113,11 @@ __device__ __forceinline__ float2 seg10s(const float w[10], const float2* arr, i
     return acc;
 }
 
-__device__ __forceinline__ void load_w10(const float* w, float wv[10]) {
-    const float2* w2 = reinterpret_cast<const float2*>(w);
+// the ten taps of target ij from the tap-major planes
+__device__ __forceinline__ void load_w10(const float2* __restrict__ w, size_t L2, size_t ij, float wv[10]) {
 #pragma unroll
     for (int d = 0; d < 5; ++d) {
-        const float2 q = __ldg(w2 + d);
+        const float2 q = __ldg(w + d * L2 + ij);
         wv[2 * d] = q.x;
         wv[2 * d + 1] = q.y;
     }
@@ -215,7 +210,7 @@ constexpr int RED_CAP = 512;  // per-warp partial sums held between folds (doubl
 struct RowShared {
     float c[4];            // B1 Hermite constants of the row (FP32)
     int bi[2];             // B1 floor index, cubic flag
-    double red[RED_CAP];   // [chunk slot][warp][8] partial sums
+    float2 red[RED_CAP];   // [chunk slot][warp][8] partial sums as (hi, lo)
 };
 
 // Row set-up for target row i: stages the last history row (FP32 mirror) in
@@ -285,6 +280,7 @@ template <int M, int K, int P, int P2>
 __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, const int ch, const int slot,
                                            const float2* s_lastf, RowShared& sh, const int i) {
     const int L = c.L, tpb = blockDim.x;
+    const size_t L2 = (size_t)L * L;
     const int nrows = sp.nrows;
     const double t = sp.T;
     const bool live = t > 0.0;
@@ -309,13 +305,13 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
             if (live) {
                 if constexpr (M == 10) {
                     float wv[10];
-                    load_w10(c.wA1f + ij * 10, wv);
+                    load_w10(c.wA1f, L2, ij, wv);
                     a1 = seg10s(wv, s_lastf, __ldg(c.iA1 + ij));
-                    load_w10(c.wA2f + ij * 10, wv);
+                    load_w10(c.wA2f, L2, ij, wv);
                     a2 = seg10s(wv, s_lastf, __ldg(c.iA2 + ij));
                 } else {
-                    a1 = dotf<M>(c.wA1f + ij * m, s_lastf + __ldg(c.iA1 + ij), m, false);
-                    a2 = dotf<M>(c.wA2f + ij * m, s_lastf + __ldg(c.iA2 + ij), m, false);
+                    a1 = dotfT(c.wA1f, L2, ij, s_lastf + __ldg(c.iA1 + ij), m, false);
+                    a2 = dotfT(c.wA2f, L2, ij, s_lastf + __ldg(c.iA2 + ij), m, false);
                 }
                 {
                     const float2 x0 = __ldg(c.KRf + (size_t)(F - 1) * L + j);
@@ -337,21 +333,20 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
                     if (X < 1) { x -= (float)(1 - X); X = 1; }
                     const float x2 = x * x, x3 = x2 * x;
                     const size_t base = (size_t)(X - 1) * L + __ldg(c.iB2 + ij);
-                    const float* w = c.wB2f + ij * m;
                     float2 S0, S1, D1, D2 = make_float2(0.f, 0.f);
                     const bool cubic2 = X < nrows - 1;
                     if constexpr (M == 10) {
                         float wv[10];
-                        load_w10(w, wv);
+                        load_w10(c.wB2f, L2, ij, wv);
                         S0 = seg10(wv, c.KRf, base);
                         S1 = seg10(wv, c.KRf, base + L);
                         D1 = seg10(wv, c.dKRf, base + L);
                         if (cubic2) D2 = seg10(wv, c.dKRf, base + 2 * L);
                     } else {
-                        S0 = dotf<M>(w, c.KRf + base, m, true);
-                        S1 = dotf<M>(w, c.KRf + base + L, m, true);
-                        D1 = dotf<M>(w, c.dKRf + base + L, m, true);
-                        if (cubic2) D2 = dotf<M>(w, c.dKRf + base + 2 * L, m, true);
+                        S0 = dotfT(c.wB2f, L2, ij, c.KRf + base, m, true);
+                        S1 = dotfT(c.wB2f, L2, ij, c.KRf + base + L, m, true);
+                        D1 = dotfT(c.wB2f, L2, ij, c.dKRf + base + L, m, true);
+                        if (cubic2) D2 = dotfT(c.wB2f, L2, ij, c.dKRf + base + 2 * L, m, true);
                     }
                     if (cubic2) {
                         const float e0 = 1.f - 3.f * x2 + 2.f * x3, e1 = x - 2.f * x2 + x3;
@@ -378,20 +373,20 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
             const float sRB2 = dB2 * b2.y;
             const float wj = __ldg(c.integ_f + j);
             const float wRA2 = wj * sRA2, wQRA2 = wj * a2.y;
-            two_sum_add(acc[0], cmp[0], wRA2 * b2.x);
-            two_sum_add(acc[1], cmp[1], (wj * sRA1) * b1.x);
-            two_sum_add(acc[2], cmp[2], (wj * sKA1) * b1.y);
-            two_sum_add(acc[3], cmp[3], wQRA2 * sKB2);
-            two_sum_add(acc[4], cmp[4], (wj * a1.y) * sKB1);
-            two_sum_add(acc[5], cmp[5], (wj * a1.x) * sRB1);
-            two_sum_add(acc[6], cmp[6], wRA2 * b2.y);
-            two_sum_add(acc[7], cmp[7], wQRA2 * sRB2);
+            const float v[8] = {wRA2 * b2.x, (wj * sRA1) * b1.x, (wj * sKA1) * b1.y, wQRA2 * sKB2,
+                                (wj * a1.y) * sKB1, (wj * a1.x) * sRB1, wRA2 * b2.y, wQRA2 * sRB2};
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                // the first term of a TwoSum from zero is exact: (s, c) = (v, 0)
+                if (kk == 0) acc[k] = v[k];
+                else two_sum_add(acc[k], cmp[k], v[k]);
+            }
         }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float H, Lo;
     warp_reduce8_pair(acc, cmp, lane, H, Lo);
-    if ((lane & 3) == 0) sh.red[((slot * (tpb >> 5)) + warp) * 8 + warp_reduce8_index(lane)] = (double)H + (double)Lo;
+    if ((lane & 3) == 0) sh.red[((slot * (tpb >> 5)) + warp) * 8 + warp_reduce8_index(lane)] = make_float2(H, Lo);
 }
 
 // After a __syncthreads() that follows chunk_sums of slots 0..ng-1 (chunks
@@ -403,7 +398,10 @@ __device__ __forceinline__ void fold_chunks(const DevCtx& c, const int i, const 
     for (int t = threadIdx.x; t < 8 * ng; t += blockDim.x) {
         const int g = t >> 3, k = t & 7;
         double sum = 0.0;
-        for (int w = 0; w < nw; ++w) sum += sh.red[(g * nw + w) * 8 + k];
+        for (int w = 0; w < nw; ++w) {
+            const float2 hl = sh.red[(g * nw + w) * 8 + k];
+            sum += (double)hl.x + (double)hl.y;
+        }
         c.part[((size_t)i * nch + ch0 + g) * 8 + k] = sum;
     }
 }
