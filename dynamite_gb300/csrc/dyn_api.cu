@@ -112,6 +112,11 @@ struct Ctx {
         // +16 elements: the 16-byte segment loads of the mixed kernel may touch
         // one element past the end of the last row
         if (d.mixed && ((s = dalloc(&KRf, ncap * L + 16)) || (s = dalloc(&dKRf, ncap * L + 16)))) return s;
+        // rows not written yet meet the zero taps of the gather segments: keep them finite
+        if (d.mixed) {
+            CK(cudaMemsetAsync(KRf, 0, (ncap * L + 16) * sizeof(float2), st));
+            CK(cudaMemsetAsync(dKRf, 0, (ncap * L + 16) * sizeof(float2), st));
+        }
         if (n && d.mixed) {
             CK(cudaMemcpyAsync(KRf, d.KRf, n * L * sizeof(float2), cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(dKRf, d.dKRf, n * L * sizeof(float2), cudaMemcpyDeviceToDevice, st));

@@ -227,6 +227,9 @@ __device__ void finish_step(const Quench& q, Plan& pl, const StageDev& last, con
 #ifndef DYN_BATCH_TPSM
 #define DYN_BATCH_TPSM 1280
 #endif
+#ifndef DYN_BATCH_SHIFT
+#define DYN_BATCH_SHIFT 0
+#endif
 template <int M, int K, int P, int P2, int TPB>
 __global__ void __launch_bounds__(TPB, (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
     k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,
@@ -253,7 +256,8 @@ __global__ void __launch_bounds__(TPB, (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
             const int nch = q.c.nch;
             for (int ch0 = 0; ch0 < nch; ch0 += GMAX) {
                 const int ng = min(GMAX, nch - ch0);
-                for (int g = 0; g < ng; ++g) mixed::chunk_sums<M, K, P, P2>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
+                for (int g = 0; g < ng; ++g)
+                    mixed::chunk_sums<M, K, P, P2, DYN_BATCH_SHIFT != 0>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
                 __syncthreads();
                 mixed::fold_chunks(q.c, i, nch, ch0, ng, sh);
                 if (ch0 + GMAX < nch) __syncthreads();
@@ -558,7 +562,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         const size_t L = grids[g].len, m = grids[g].depth, L2 = L * L;
         gd.L = L;
         gd.m = m;
-        all10 = all10 && m == 10;
+        all10 = all10 && m == 10 && L % 2 == 0;  // depth-10 kernels need an even L
         bt->Lmax = std::max(bt->Lmax, L);
         std::vector<int> i32[3];
         std::string why;

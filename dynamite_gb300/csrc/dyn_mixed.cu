@@ -52,7 +52,8 @@ cudaError_t launch_k(const DevCtx& c, int s, cudaStream_t st) {
 
 template <int P, int P2>
 cudaError_t launch_pp(const DevCtx& c, int s, cudaStream_t st) {
-    return c.m == 10 ? launch_k<10, P, P2>(c, s, st) : launch_k<0, P, P2>(c, s, st);
+    // the depth-10 kernels lay the weights over element pairs: they need an even L
+    return (c.m == 10 && c.L % 2 == 0) ? launch_k<10, P, P2>(c, s, st) : launch_k<0, P, P2>(c, s, st);
 }
 
 __global__ void k_to_f32(const double2* in, float2* out, size_t count) {

@@ -66,10 +66,10 @@ __device__ __forceinline__ float2 dotfT(const float2* __restrict__ w, size_t L2,
     return acc;
 }
 
-// sum_d w[d] * x[b + d] for a 10-tap row segment of float2 elements, read as
-// six 16-byte loads from the 16-byte boundary at or below b (element pairs)
-// instead of ten 8-byte loads: each vector load is one L1 wavefront per lane
-// on these scattered rows, which is what bounds this kernel.
+// sum_d w[d] * x[b + d] for a 10-tap segment read as six 16-byte loads from
+// the even element at or below b, each tap selecting its element (the select
+// form; the same sums as seg11 with shifted weights, up to the sign of an
+// exact zero, with fewer live registers)
 __device__ __forceinline__ float2 seg10(const float w[10], const float2* __restrict__ arr, size_t b) {
     const size_t a = b & ~(size_t)1;
     const bool sh = b & 1;
@@ -90,8 +90,6 @@ __device__ __forceinline__ float2 seg10(const float w[10], const float2* __restr
     }
     return acc;
 }
-
-// The same 10-tap segment from shared memory (the staged last row)
 __device__ __forceinline__ float2 seg10s(const float w[10], const float2* arr, int b) {
     const int a = b & ~1;
     const bool sh = b & 1;
@@ -110,6 +108,56 @@ __device__ __forceinline__ float2 seg10s(const float w[10], const float2* arr, i
         acc.x = fmaf(w[d], x.x, acc.x);
         acc.y = fmaf(w[d], x.y, acc.y);
     }
+    return acc;
+}
+
+// The ten stencil weights laid over the element pairs that start at the even
+// element a = b & ~1 at or below the stencil start b: w11[k] = w[k - (b & 1)]
+// (zero outside 0..9).  A segment sum then needs no per-element select, and
+// one shift serves every segment whose start has the same parity.
+__device__ __forceinline__ void shift_w(const float w[10], const bool sh, float w11[11]) {
+    w11[0] = sh ? 0.f : w[0];
+#pragma unroll
+    for (int k = 1; k < 10; ++k) w11[k] = sh ? w[k - 1] : w[k];
+    w11[10] = sh ? w[9] : 0.f;
+}
+
+// sum_k w11[k] * arr[a + k], k = 0..10, a even: five 16-byte loads and one
+// 8-byte load, taps in order.  The zero tap leaves the sum of the ten others
+// unchanged, so arr[a .. a+10] must be finite (history mirrors and the staged
+// row are zero-filled past what has been written).
+__device__ __forceinline__ float2 seg11(const float w11[11], const float2* __restrict__ arr, size_t a) {
+    const float4* p = reinterpret_cast<const float4*>(arr + a);
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const float4 v = __ldg(p + q);
+        acc.x = fmaf(w11[2 * q], v.x, acc.x);
+        acc.y = fmaf(w11[2 * q], v.y, acc.y);
+        acc.x = fmaf(w11[2 * q + 1], v.z, acc.x);
+        acc.y = fmaf(w11[2 * q + 1], v.w, acc.y);
+    }
+    const float2 e = __ldg(arr + a + 10);
+    acc.x = fmaf(w11[10], e.x, acc.x);
+    acc.y = fmaf(w11[10], e.y, acc.y);
+    return acc;
+}
+
+// The same segment from shared memory (the staged last row)
+__device__ __forceinline__ float2 seg11s(const float w11[11], const float2* arr, int a) {
+    const float4* p = reinterpret_cast<const float4*>(arr + a);
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const float4 v = p[q];
+        acc.x = fmaf(w11[2 * q], v.x, acc.x);
+        acc.y = fmaf(w11[2 * q], v.y, acc.y);
+        acc.x = fmaf(w11[2 * q + 1], v.z, acc.x);
+        acc.y = fmaf(w11[2 * q + 1], v.w, acc.y);
+    }
+    const float2 e = arr[a + 10];
+    acc.x = fmaf(w11[10], e.x, acc.x);
+    acc.y = fmaf(w11[10], e.y, acc.y);
     return acc;
 }
 
@@ -174,7 +222,7 @@ __device__ __forceinline__ void warp_reduce8_pair(const float hv[8], const float
 // Binary search of bsearchPosSorted (the same probes as pos_binary), returning
 // floor(position) as an integer and the offset from it in FP32.
 __device__ __forceinline__ void pos_split(const ListView& L, const float* __restrict__ inv_len, double El,
-                                          long long& X, float& x) {
+                                          int& X, float& x) {
     int n0 = 1, n1 = L.n, m = 1;
     double Lm = 0.0;
     const long long kE = okey(El);
@@ -276,7 +324,9 @@ __device__ __forceinline__ void row_setup(const DevCtx& c, const StageDev& sp, c
 // TwoSum accumulation; each warp's eight sums land in sh.red[slot][warp].
 // Call after row_setup and a __syncthreads(); no barrier inside, so a block
 // can run several chunks (slots) before one fold.
-template <int M, int K, int P, int P2>
+// SHIFT picks the segment form for depth 10 (shifted weights, seg11, or
+// per-tap selects, seg10): same results, different register footprints.
+template <int M, int K, int P, int P2, bool SHIFT = true>
 __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, const int ch, const int slot,
                                            const float2* s_lastf, RowShared& sh, const int i) {
     const int L = c.L, tpb = blockDim.x;
@@ -303,7 +353,16 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
             const size_t ij = (size_t)i * L + j;
             float2 a1, a2, b1, b2;
             if (live) {
-                if constexpr (M == 10) {
+                if constexpr (M == 10 && SHIFT) {
+                    float wv[10], w11[11];
+                    const int sa1 = __ldg(c.iA1 + ij), sa2 = __ldg(c.iA2 + ij);
+                    load_w10(c.wA1f, L2, ij, wv);
+                    shift_w(wv, sa1 & 1, w11);
+                    a1 = seg11s(w11, s_lastf, sa1 & ~1);
+                    load_w10(c.wA2f, L2, ij, wv);
+                    shift_w(wv, sa2 & 1, w11);
+                    a2 = seg11s(w11, s_lastf, sa2 & ~1);
+                } else if constexpr (M == 10) {
                     float wv[10];
                     load_w10(c.wA1f, L2, ij, wv);
                     a1 = seg10s(wv, s_lastf, __ldg(c.iA1 + ij));
@@ -326,16 +385,26 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
                     }
                 }
                 {
-                    long long X;
+                    int X;
                     float x;
                     pos_split(lv, c.inv_len_f, __dmul_rn(__ldg(c.phi2 + ij), t), X, x);
-                    if (X > maxX) { x += (float)(X - maxX); X = maxX; }
-                    if (X < 1) { x -= (float)(1 - X); X = 1; }
+                    if (X > maxX) { x += __int2float_rn(X - maxX); X = maxX; }
+                    if (X < 1) { x -= __int2float_rn(1 - X); X = 1; }
                     const float x2 = x * x, x3 = x2 * x;
-                    const size_t base = (size_t)(X - 1) * L + __ldg(c.iB2 + ij);
+                    const size_t base = (size_t)(X - 1) * (size_t)L + (size_t)__ldg(c.iB2 + ij);
                     float2 S0, S1, D1, D2 = make_float2(0.f, 0.f);
                     const bool cubic2 = X < nrows - 1;
-                    if constexpr (M == 10) {
+                    if constexpr (M == 10 && SHIFT) {
+                        // even L (the M == 10 kernels require it): every segment start has base's parity
+                        float wv[10], w11[11];
+                        load_w10(c.wB2f, L2, ij, wv);
+                        shift_w(wv, base & 1, w11);
+                        const size_t a = base & ~(size_t)1;
+                        S0 = seg11(w11, c.KRf, a);
+                        S1 = seg11(w11, c.KRf, a + L);
+                        D1 = seg11(w11, c.dKRf, a + L);
+                        if (cubic2) D2 = seg11(w11, c.dKRf, a + 2 * L);
+                    } else if constexpr (M == 10) {
                         float wv[10];
                         load_w10(c.wB2f, L2, ij, wv);
                         S0 = seg10(wv, c.KRf, base);
@@ -397,12 +466,13 @@ __device__ __forceinline__ void fold_chunks(const DevCtx& c, const int i, const 
     const int nw = blockDim.x >> 5;
     for (int t = threadIdx.x; t < 8 * ng; t += blockDim.x) {
         const int g = t >> 3, k = t & 7;
-        double sum = 0.0;
+        // warps in order, compensated on the high parts; one conversion at the end
+        float h = 0.f, l = 0.f;
         for (int w = 0; w < nw; ++w) {
             const float2 hl = sh.red[(g * nw + w) * 8 + k];
-            sum += (double)hl.x + (double)hl.y;
+            pair_add(h, l, hl.x, hl.y);
         }
-        c.part[((size_t)i * nch + ch0 + g) * 8 + k] = sum;
+        c.part[((size_t)i * nch + ch0 + g) * 8 + k] = (double)h + (double)l;
     }
 }
 
