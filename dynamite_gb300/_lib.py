@@ -108,6 +108,16 @@ class BatchInfo(C.Structure):
     ]
 
 
+class AdjointObjective(C.Structure):
+    _fields_ = [("w_energy", C.c_double), ("w_r", C.c_double), ("c_K", dp), ("c_R", dp), ("c_dK", dp),
+                ("c_dR", dp), ("w_dr", C.c_double)]
+
+
+class AdjointStats(C.Structure):
+    _fields_ = [("ms_forward", C.c_double), ("ms_backward", C.c_double), ("device_bytes", C.c_size_t),
+                ("steps", C.c_int), ("recompute_mismatch", C.c_longlong)]
+
+
 DYN_QUENCH_RUNNING, DYN_QUENCH_DONE, DYN_QUENCH_MAXSTEPS, DYN_QUENCH_FULL = 0, 1, 2, 3
 
 _lib = None
@@ -167,6 +177,9 @@ def lib():
             "dyn_batch_last_row": ([vp, C.c_int, dp, dp], C.c_int),
             "dyn_batch_tune": ([vp, C.c_int, ip, ip, ip, C.POINTER(C.c_float)], C.c_int),
             "dyn_batch_profile": ([vp, C.c_int, C.POINTER(C.c_float)], C.c_int),
+            "dyn_adjoint_forward": ([vp, C.POINTER(RunParams), C.POINTER(StepResult)], C.c_int),
+            "dyn_adjoint_backward": ([vp, C.POINTER(AdjointObjective), dp, C.POINTER(AdjointStats)], C.c_int),
+            "dyn_adjoint_history_grad": ([vp, C.POINTER(StateC)], C.c_int),
             "dyn_grid_generate": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                    dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
         }

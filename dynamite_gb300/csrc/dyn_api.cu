@@ -7,6 +7,7 @@
 // size L or L^2 lives on the device.  One RK step is one H2D copy of the
 // stage descriptors, 2 kernels per stage, and one D2H copy of the step result,
 // optionally replayed as a CUDA graph.
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -66,6 +67,21 @@ struct Ctx {
     std::map<int, cudaGraphExec_t> graphs;
     std::map<int, int> warm;
     bool interp_alloc = false;
+    unsigned long long gen = 0;  // bumped by every change of the history
+    // discrete adjoint (FP64, fixed schedule): the recorded forward and its buffers
+    AdjDev ad{};
+    size_t ad_cap = 0;
+    double* ad_ck = nullptr;        // [4][L] objective weights on the final row (K, R, dK, dR)
+    double2* snap_KR = nullptr;     // history snapshot restored after the reverse sweep
+    double2* snap_dKR = nullptr;
+    double* snap_time = nullptr;    // [5][cap]: t1grid, dtr, inv_dtr, rvec, drvec
+    bool adj_recorded = false;
+    unsigned long long adj_gen = 0;
+    size_t adj_n_start = 0;
+    std::vector<double> adj_dt;
+    std::vector<int> adj_method;
+    double adj_ms_forward = 0.0;
+    cudaEvent_t stages_copied = nullptr;  // the last async copy out of stages_h has run
 
     ~Ctx() { release(); }
 
@@ -74,8 +90,22 @@ struct Ctx {
         graphs.clear();
     }
 
+    void release_adjoint() {
+        void* ab[] = {ad.HKR, ad.HdKR, ad.Hr, ad.Hdr, ad.Gsave, ad.Dsave, ad.rsave, ad.drsave, ad.Psave, ad.hbar,
+                      ad.g0bar, ad.Gbar, ad.Dbar, ad.abar, ad.lbar_part, ad.sc, ad_ck, snap_KR, snap_dKR, snap_time};
+        for (void* b : ab) if (b) cudaFree(b);
+        std::memset(&ad, 0, sizeof ad);
+        ad_ck = nullptr;
+        snap_KR = snap_dKR = nullptr;
+        snap_time = nullptr;
+        ad_cap = 0;
+    }
+
     void release() {
         drop_graphs();
+        release_adjoint();
+        if (stages_copied) cudaEventDestroy(stages_copied);
+        stages_copied = nullptr;
         void* bufs[] = {(void*)d.theta, (void*)d.phi2, (void*)d.integ, (void*)d.iA1, (void*)d.iA2, (void*)d.iB2,
                         (void*)d.wA1, (void*)d.wA2, (void*)d.wB2, d.KR, d.dKR, d.t1grid, d.dtr, d.inv_dtr,
                         d.rvec, d.drvec, d.posB1x, d.posB1x_next, d.posB1x_saved, d.posB2x, d.posB2x_saved, d.h, d.gS,
@@ -315,6 +345,7 @@ struct Ctx {
         t1.push_back(Tf);
         dtr.push_back(dtrf);
         n += 1;
+        gen++;
         if (res) {
             res->delta = slots_h->res_err + err_t;
             res->t = Tf;
@@ -322,6 +353,84 @@ struct Ctx {
             res->energy = slots_h->res_energy;
             res->qk0 = slots_h->res_qk0;
             res->dr = slots_h->res_dr;
+        }
+        return DYN_OK;
+    }
+
+    // ---------------------------------------------------------- adjoint
+    dyn_status adjoint_alloc() {
+        if (ad_cap == cap && ad.HKR) return DYN_OK;
+        release_adjoint();
+        const size_t Lz = L;
+        dyn_status s;
+        if ((s = dalloc(&ad.HKR, cap * Lz)) || (s = dalloc(&ad.HdKR, cap * Lz)) || (s = dalloc(&ad.Hr, cap)) ||
+            (s = dalloc(&ad.Hdr, cap)) || (s = dalloc(&ad.Gsave, (size_t)SMAX * Lz)) ||
+            (s = dalloc(&ad.Dsave, (size_t)SMAX * Lz)) || (s = dalloc(&ad.rsave, SMAX)) || (s = dalloc(&ad.drsave, SMAX)) ||
+            (s = dalloc(&ad.Psave, (size_t)SMAX * Lz)) || (s = dalloc(&ad.hbar, (size_t)SMAX * Lz)) ||
+            (s = dalloc(&ad.g0bar, Lz)) || (s = dalloc(&ad.Gbar, Lz)) || (s = dalloc(&ad.Dbar, Lz)) ||
+            (s = dalloc(&ad.abar, 8 * Lz)) || (s = dalloc(&ad.lbar_part, Lz * Lz)) || (s = dalloc(&ad.sc, 16)) ||
+            (s = dalloc(&ad_ck, 4 * Lz)) || (s = dalloc(&snap_KR, cap * Lz)) || (s = dalloc(&snap_dKR, cap * Lz)) ||
+            (s = dalloc(&snap_time, 5 * cap))) {
+            release_adjoint();
+            return s;
+        }
+        CK(adj_targets_smem_attr(L));
+        ad_cap = cap;
+        return DYN_OK;
+    }
+
+    size_t adjoint_bytes() const {
+        const size_t Lz = L;
+        return (cap * Lz * 2 * sizeof(double2)) * 2 + cap * 2 * sizeof(double) + 5 * cap * sizeof(double) +
+               (size_t)SMAX * Lz * (3 * sizeof(double2) + sizeof(double)) + Lz * Lz * sizeof(double2) +
+               Lz * (3 * sizeof(double2) + 9 * sizeof(double)) + 2 * SMAX * sizeof(double) + 16 * sizeof(double);
+    }
+
+    // Step n0 -> n0 + 1 again from the history prefix (same kernels, same
+    // stage descriptors as the forward), keeping what the reverse sweep needs
+    // of each stage: the B1 positions it read and row n0 after it.
+    dyn_status recompute_step(int method, double dt, int* S_out) {
+        // stages_h is the source of an asynchronous copy: the previous step's
+        // copy must have run before the records are rewritten
+        if (!stages_copied) CK(cudaEventCreateWithFlags(&stages_copied, cudaEventDisableTiming));
+        else CK(cudaEventSynchronize(stages_copied));
+        int S;
+        double err_t, Tf, dtrf;
+        dyn_status s = build_step(method, dt, &S, &err_t, &Tf, &dtrf);
+        if (s) return s;
+        const size_t n0 = n, Lz = L;
+        CK(launch_pos_init(d, (int)n0, st));
+        CK(cudaMemcpyAsync(d.stages, stages_h, sizeof(StageDev) * S, cudaMemcpyHostToDevice, st));
+        CK(cudaEventRecord(stages_copied, st));
+        for (int k = 0; k < S; ++k) {
+            CK(cudaMemcpyAsync(ad.Psave + k * Lz, d.posB1x, Lz * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            CK(launch_stage(d, k, st));
+            CK(cudaMemcpyAsync(ad.Gsave + k * Lz, d.KR + n0 * Lz, Lz * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(ad.Dsave + k * Lz, d.dKR + n0 * Lz, Lz * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(ad.rsave + k, d.rvec + n0, sizeof(double), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(ad.drsave + k, d.drvec + n0, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        }
+        t1.push_back(Tf);
+        dtr.push_back(dtrf);
+        n += 1;
+        *S_out = S;
+        return DYN_OK;
+    }
+
+    dyn_status snapshot(bool restore) {
+        const size_t rows = n, Lz = L;
+        auto cp = [&](void* dst, const void* src, size_t bytes) {
+            return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+        };
+        double* tv[5] = {d.t1grid, d.dtr, d.inv_dtr, d.rvec, d.drvec};
+        if (!restore) {
+            CK(cp(snap_KR, d.KR, rows * Lz * sizeof(double2)));
+            CK(cp(snap_dKR, d.dKR, rows * Lz * sizeof(double2)));
+            for (int k = 0; k < 5; ++k) CK(cp(snap_time + k * cap, tv[k], rows * sizeof(double)));
+        } else {
+            CK(cp(d.KR, snap_KR, rows * Lz * sizeof(double2)));
+            CK(cp(d.dKR, snap_dKR, rows * Lz * sizeof(double2)));
+            for (int k = 0; k < 5; ++k) CK(cp(tv[k], snap_time + k * cap, rows * sizeof(double)));
         }
         return DYN_OK;
     }
@@ -541,6 +650,7 @@ dyn_status dyn_state_init(void* p, double delta_t) {
     Ctx* c = C(p);
     const int L = c->L;
     c->n = 1;
+    c->gen++;
     c->t1.assign(1, 0.0);
     c->dtr.assign(1, 0.0);
     std::vector<double2> row(L, make_double2(1.0, 1.0)), zero(L, make_double2(0.0, 0.0));
@@ -574,6 +684,7 @@ dyn_status dyn_state_upload(void* p, const dyn_state* stt) {
         if (k && !(stt->t1grid[k] >= stt->t1grid[k - 1])) return fail(DYN_ERR_INVALID, "t1grid must be non-decreasing");
     }
     c->drop_graphs();
+    c->gen++;
     c->n = 0;
     dyn_status s = c->ensure_rows(n + 1);
     if (s) return s;
@@ -833,6 +944,7 @@ dyn_status dyn_rollback(void* p, int nrows) {
     if (nrows < 0 || (size_t)nrows >= c->n - 1) return fail(DYN_ERR_INVALID, "cannot roll back that many rows");
     const size_t target = c->n - nrows;
     c->n = target;
+    c->gen++;
     c->t1.resize(target);
     c->dtr.resize(target);
     c->ctl.delta_t = c->t1[target - 1] - c->t1[target - 2];
@@ -925,6 +1037,125 @@ dyn_status dyn_probe_fp64(int device, double* gflops) {
 
 // sparsifyNscale / sparsifyNscaleGPU: device indicator per node, host index
 // logic of the selected variant, one device compaction pass.
+// ------------------------------------------------------------------ adjoint
+dyn_status dyn_adjoint_forward(void* p, const dyn_run_params* rp, dyn_step_result* last) {
+    if (!p || !rp) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (c->d.mixed) return fail(DYN_ERR_UNSUPPORTED, "the adjoint runs on the FP64 form");
+    if (rp->gpu_rollback) return fail(DYN_ERR_INVALID, "the adjoint needs an append-only history: no rollback");
+    if (c->n == 0) return fail(DYN_ERR_STATE, "no state: call dyn_state_init or dyn_state_upload");
+    if (rp->nsteps < 0) return fail(DYN_ERR_INVALID, "nsteps must be non-negative");
+    const size_t N = (size_t)rp->nsteps;
+    std::vector<double> dts(N);
+    std::vector<int> ms(N);
+    dyn_run_params q = *rp;
+    q.out_dt = dts.data();
+    q.out_method = ms.data();
+    const size_t n_start = c->n;
+    c->adj_recorded = false;
+    const auto t0 = std::chrono::steady_clock::now();
+    dyn_status s = dyn_run(p, &q, last);
+    if (s) return s;
+    CK(cudaStreamSynchronize(c->st));
+    const auto t1 = std::chrono::steady_clock::now();
+    const size_t ran = c->n - n_start;
+    dts.resize(ran);
+    ms.resize(ran);
+    if (rp->out_dt) std::memcpy(rp->out_dt, dts.data(), ran * sizeof(double));
+    if (rp->out_method) std::memcpy(rp->out_method, ms.data(), ran * sizeof(int));
+    c->adj_dt = std::move(dts);
+    c->adj_method = std::move(ms);
+    c->adj_n_start = n_start;
+    c->adj_gen = c->gen;
+    c->adj_recorded = true;
+    c->adj_ms_forward = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    return DYN_OK;
+}
+
+dyn_status dyn_adjoint_backward(void* p, const dyn_adjoint_objective* obj, double* grad, dyn_adjoint_stats* stats) {
+    if (!p || !obj || !grad) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (!c->adj_recorded || c->gen != c->adj_gen)
+        return fail(DYN_ERR_STATE, "no recorded forward: call dyn_adjoint_forward (the history changed since)");
+    for (int m : c->adj_method)
+        if (m != DYN_RK54 && m != DYN_SSPRK104) return fail(DYN_ERR_UNSUPPORTED, "adjoint of SERK2 steps is not built");
+    dyn_status s = c->adjoint_alloc();
+    if (s) return s;
+    const auto t0 = std::chrono::steady_clock::now();
+    const size_t n_final = c->n, N = c->adj_dt.size(), L = c->L;
+    const std::vector<double> t1_saved = c->t1, dtr_saved = c->dtr;
+    if ((s = c->snapshot(false))) return s;
+    CK(cudaMemsetAsync(c->ad.HKR, 0, n_final * L * sizeof(double2), c->st));
+    CK(cudaMemsetAsync(c->ad.HdKR, 0, n_final * L * sizeof(double2), c->st));
+    CK(cudaMemsetAsync(c->ad.Hr, 0, n_final * sizeof(double), c->st));
+    CK(cudaMemsetAsync(c->ad.Hdr, 0, n_final * sizeof(double), c->st));
+    CK(cudaMemsetAsync(c->ad.sc, 0, 16 * sizeof(double), c->st));
+    const AdjModel am{c->cfg.p, c->cfg.p2, c->cfg.lambda, c->cfg.T0, c->cfg.Gamma};
+    const double* seeds[4] = {obj->c_K, obj->c_R, obj->c_dK, obj->c_dR};
+    const double* dseeds[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < 4; ++k) {
+        if (!seeds[k]) continue;
+        CK(cudaMemcpyAsync(c->ad_ck + k * L, seeds[k], L * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        dseeds[k] = c->ad_ck + k * L;
+    }
+    CK(launch_adj_seed(c->d, c->ad, am, (int)n_final - 1, obj->w_energy, obj->w_r, obj->w_dr, dseeds[0], dseeds[1],
+                       dseeds[2], dseeds[3], c->st));
+    for (size_t k = N; k-- > 0;) {
+        const size_t n0 = c->adj_n_start + k;
+        c->n = n0;
+        c->t1.resize(n0);
+        c->dtr.resize(n0);
+        int S;
+        if ((s = c->recompute_step(c->adj_method[k], c->adj_dt[k], &S))) return s;
+        CK(launch_adj_verify(c->d, c->ad, c->snap_KR, c->snap_dKR, c->snap_time + 3 * c->cap, c->snap_time + 4 * c->cap,
+                             (int)n0, c->st));
+        CK(launch_adj_step(c->d, c->ad, am, S, (int)n0, c->st));
+    }
+    if (c->adj_n_start == 1) CK(launch_adj_initial(c->ad, am, c->st));
+    double sc[16];
+    CK(cudaMemcpyAsync(sc, c->ad.sc, sizeof sc, cudaMemcpyDeviceToHost, c->st));
+    // the history back as the forward left it
+    c->n = n_final;
+    c->t1 = t1_saved;
+    c->dtr = dtr_saved;
+    if ((s = c->snapshot(true))) return s;
+    if ((s = c->pos_init())) return s;
+    CK(cudaStreamSynchronize(c->st));
+    const auto t1 = std::chrono::steady_clock::now();
+    grad[0] = sc[3];
+    grad[1] = sc[4];
+    if (stats) {
+        stats->ms_forward = c->adj_ms_forward;
+        stats->ms_backward = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        stats->device_bytes = c->adjoint_bytes();
+        stats->steps = (int)N;
+        stats->recompute_mismatch = (long long)sc[15];
+    }
+    return DYN_OK;
+}
+
+dyn_status dyn_adjoint_history_grad(void* p, dyn_state* g) {
+    if (!p || !g) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (!c->ad.HKR || !c->adj_recorded) return fail(DYN_ERR_STATE, "call dyn_adjoint_backward first");
+    const size_t n = c->adj_n_start, L = c->L;
+    if (g->n < n) return fail(DYN_ERR_INVALID, "gradient buffers hold fewer rows than the initial history");
+    g->n = n;
+    std::vector<double2> kr(n * L), dkr(n * L);
+    CK(cudaMemcpyAsync(kr.data(), c->ad.HKR, n * L * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(dkr.data(), c->ad.HdKR, n * L * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+    if (g->rvec) CK(cudaMemcpyAsync(g->rvec, c->ad.Hr, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    if (g->drvec) CK(cudaMemcpyAsync(g->drvec, c->ad.Hdr, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t e = 0; e < n * L; ++e) {
+        if (g->QK) g->QK[e] = kr[e].x;
+        if (g->QR) g->QR[e] = kr[e].y;
+        if (g->dQK) g->dQK[e] = dkr[e].x;
+        if (g->dQR) g->dQR[e] = dkr[e].y;
+    }
+    return DYN_OK;
+}
+
 dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
     if (!p) return fail(DYN_ERR_INVALID, "null ctx");
     if (variant < 0 || variant > 2) return fail(DYN_ERR_INVALID, "unknown sparsify variant");
@@ -1008,6 +1239,7 @@ dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
     c->t1 = t1n;
     c->dtr = dtrn;
     c->n = k;
+    c->gen++;
     if ((s = c->mirror_all())) return s;
     if ((s = c->upload_times())) return s;
     if ((s = c->pos_init())) return s;

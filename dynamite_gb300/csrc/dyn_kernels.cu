@@ -24,85 +24,6 @@
 
 namespace dyn {
 
-// sum_d w[d] * x[d] for K and R together (x interleaved)
-template <int M>
-__device__ __forceinline__ double2 dot2g(const double* __restrict__ w, const double2* __restrict__ x, int m) {
-    double2 acc = make_double2(0.0, 0.0);
-    if constexpr (M > 0 && (M % 2) == 0) {
-        const double2* w2 = reinterpret_cast<const double2*>(w);
-#pragma unroll
-        for (int d = 0; d < M / 2; ++d) {
-            const double2 ww = __ldg(w2 + d);
-            const double2 xa = __ldg(x + 2 * d), xb = __ldg(x + 2 * d + 1);
-            acc.x = fma(ww.x, xa.x, acc.x);
-            acc.y = fma(ww.x, xa.y, acc.y);
-            acc.x = fma(ww.y, xb.x, acc.x);
-            acc.y = fma(ww.y, xb.y, acc.y);
-        }
-    } else {
-        for (int d = 0; d < m; ++d) {
-            const double ww = __ldg(w + d);
-            const double2 xa = __ldg(x + d);
-            acc.x = fma(ww, xa.x, acc.x);
-            acc.y = fma(ww, xa.y, acc.y);
-        }
-    }
-    return acc;
-}
-
-template <int M>
-__device__ __forceinline__ double2 dot2s(const double* __restrict__ w, const double2* x, int m) {
-    double2 acc = make_double2(0.0, 0.0);
-    if constexpr (M > 0 && (M % 2) == 0) {
-        const double2* w2 = reinterpret_cast<const double2*>(w);
-#pragma unroll
-        for (int d = 0; d < M / 2; ++d) {
-            const double2 ww = __ldg(w2 + d);
-            const double2 xa = x[2 * d], xb = x[2 * d + 1];
-            acc.x = fma(ww.x, xa.x, acc.x);
-            acc.y = fma(ww.x, xa.y, acc.y);
-            acc.x = fma(ww.y, xb.x, acc.x);
-            acc.y = fma(ww.y, xb.y, acc.y);
-        }
-    } else {
-        for (int d = 0; d < m; ++d) {
-            const double ww = __ldg(w + d);
-            const double2 xa = x[d];
-            acc.x = fma(ww, xa.x, acc.x);
-            acc.y = fma(ww, xa.y, acc.y);
-        }
-    }
-    return acc;
-}
-
-// B1 Hermite coefficients of one target row (index_vec.cu:399-441 form,
-// with the per-row division folded into c3).
-struct B1Row {
-    int F, cubic;
-    double c0, c1, c2, c3;
-};
-
-__device__ __forceinline__ B1Row b1_row(const DevCtx& c, double pos, int maxceil, int nrows) {
-    B1Row r;
-    long long F = (long long)floor(pos);
-    if (F < 1) F = 1; else if (F > maxceil) F = maxceil;
-    r.F = (int)F;
-    const double u = (double)F - pos, u2 = u * u, u3 = u2 * u;
-    r.cubic = F < nrows - 1;
-    if (r.cubic) {
-        r.c0 = 1.0 - 3.0 * u2 - 2.0 * u3;
-        r.c1 = 3.0 * u2 + 2.0 * u3;
-        r.c2 = u + 2.0 * u2 + u3;
-        r.c3 = (u2 + u3) * c.inv_dtr[F + 1];
-    } else {
-        r.c0 = 1.0 - u2;
-        r.c1 = u2;
-        r.c2 = u + u2;
-        r.c3 = 0.0;
-    }
-    return r;
-}
-
 // Position of theta_i * T_next for the next stage (the row written by this
 // stage's epilogue becomes the last list entry), computed while the gather
 // kernel runs so the epilogue only copies it.

@@ -97,6 +97,31 @@ struct DevCtx {
     double* rint;          // [L]
 };
 
+// Adjoint state of the FP64 path (dyn_adjoint.cu): cotangents of the
+// history and per-step stage snapshots from the recompute.
+struct AdjDev {
+    double2* HKR;      // [cap][L] cotangents of (QK, QR)
+    double2* HdKR;     // [cap][L] cotangents of (dQK, dQR)
+    double* Hr;        // [cap]
+    double* Hdr;       // [cap]
+    double2* Gsave;    // [SMAX][L] row n0 (QK, QR) after stage s
+    double2* Dsave;    // [SMAX][L] row n0 (dQK, dQR) after stage s
+    double* rsave;     // [SMAX] r of row n0 after stage s
+    double* drsave;    // [SMAX]
+    double* Psave;     // [SMAX][L] B1 positions stage s read
+    double2* hbar;     // [SMAX][L] cotangents of the stage right-hand sides
+    double2* g0bar;    // [L] cotangent of the step's base row
+    double2* Gbar;     // [L] cotangent of row n0's (QK, QR) after the current stage
+    double2* Dbar;     // [L]
+    double* abar;      // [L][8] cotangents of the eight memory-integral rows
+    double2* lbar_part;  // [L][L] per-target-row last-row stencil cotangents
+    double* sc;        // scalars: rho, delta, DR, Gamma, lambda
+};
+struct AdjModel {
+    int p, p2;
+    double lam, T0, Gamma;
+};
+
 // Model coefficients in the reference's host evaluation order
 // (math_ops.cpp:27-37: (lambda*p)*(p-1)... with p as the integer exponent)
 inline DModel make_model(int p, int p2, double lambda, double T0, double Gamma) {
@@ -166,5 +191,14 @@ cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* i
 cudaError_t launch_fp64_probe(double* out, int blocks, int threads, int iters, cudaStream_t st);
 cudaError_t launch_unpack_rows(const double2* in, double* QK, double* QR, size_t count,
                                cudaStream_t st);
+
+cudaError_t launch_adj_seed(const DevCtx& c, const AdjDev& a, const AdjModel& am, int nl, double wE, double wR,
+                            double wDr, const double* cK, const double* cR, const double* cdK, const double* cdR,
+                            cudaStream_t st);
+cudaError_t launch_adj_step(const DevCtx& c, const AdjDev& a, const AdjModel& am, int S, int n0, cudaStream_t st);
+cudaError_t launch_adj_initial(const AdjDev& a, const AdjModel& am, cudaStream_t st);
+cudaError_t launch_adj_verify(const DevCtx& c, const AdjDev& a, const double2* snapKR, const double2* snapdKR,
+                              const double* snapr, const double* snapdr, int n0, cudaStream_t st);
+cudaError_t adj_targets_smem_attr(int L);
 
 }  // namespace dyn

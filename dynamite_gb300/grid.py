@@ -94,3 +94,16 @@ def save(g: Grid, directory: str) -> None:
     for name, inds, w in (("A1y", g.indsA1, g.wA1), ("A2y", g.indsA2, g.wA2), ("B2y", g.indsB2, g.wB2)):
         mat(f"inds{name}.dat", inds, fmt="%d")
         vec(f"weights{name}.dat", w)
+
+
+def lagrange_weights(theta, x: float, npts: int = 10):
+    """Weights c with c . f(theta) = the degree npts-1 Lagrange interpolant of f at x on the
+    npts theta nodes nearest x (the C(t, x t) functional of a history row)."""
+    th = np.asarray(theta, dtype=np.float64)
+    k0 = int(np.clip(np.searchsorted(th, x) - npts // 2, 0, th.size - npts))
+    nodes = th[k0:k0 + npts]
+    c = np.zeros(th.size)
+    for a in range(npts):
+        others = np.delete(nodes, a)
+        c[k0 + a] = np.prod((x - others) / (nodes[a] - others))
+    return c

@@ -228,6 +228,46 @@ class Simulation:
         out["method"] = meth
         return out
 
+    # ------------------------------------------------------ discrete adjoint
+    def adjoint_forward(self, nsteps: int, schedule=None, tmax: float = 0.0) -> dict:
+        """`run` (no rollback) that records its step schedule for `adjoint_backward`."""
+        out = {k: np.zeros(nsteps) for k in ("dt", "delta", "t", "energy", "qk0", "r")}
+        meth = np.zeros(nsteps, dtype=np.int32)
+        sd = sm = None
+        if schedule is not None:
+            sd = np.ascontiguousarray(schedule[0], dtype=np.float64)
+            sm = np.ascontiguousarray(schedule[1], dtype=np.int32)
+        rp = _lib.RunParams(nsteps, tmax, _lib.ptr(sd), None if sm is None else sm.ctypes.data_as(_lib.ip), 0,
+                            _lib.ptr(out["dt"]), meth.ctypes.data_as(_lib.ip), _lib.ptr(out["delta"]),
+                            _lib.ptr(out["t"]), _lib.ptr(out["energy"]), _lib.ptr(out["qk0"]), _lib.ptr(out["r"]))
+        last = _lib.StepResult()
+        _lib.check(_lib.lib().dyn_adjoint_forward(self._h, C.byref(rp), C.byref(last)), "dyn_adjoint_forward")
+        out["method"] = meth
+        return out
+
+    def adjoint_backward(self, w_energy: float = 0.0, w_r: float = 0.0, c_K=None, c_R=None, c_dK=None, c_dR=None,
+                         w_dr: float = 0.0):
+        """Gradient (d/dGamma, d/dlambda) of w_energy E(t_f) + c_K . C(t_f, theta t_f) + w_r r(t_f)
+        (+ c_R . R, c_dK . dQK, c_dR . dQR, w_dr drvec of the final row) over the recorded forward;
+        returns (grad, stats)."""
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (c_K, c_R, c_dK, c_dR)]
+        obj = _lib.AdjointObjective(w_energy, w_r, *[_lib.ptr(a) for a in arrs], w_dr)
+        g = np.zeros(2)
+        st = _lib.AdjointStats()
+        _lib.check(_lib.lib().dyn_adjoint_backward(self._h, C.byref(obj), _lib.ptr(g), C.byref(st)),
+                   "dyn_adjoint_backward")
+        return g, dict(ms_forward=st.ms_forward, ms_backward=st.ms_backward, device_bytes=int(st.device_bytes),
+                       steps=st.steps, recompute_mismatch=int(st.recompute_mismatch))
+
+    def adjoint_history_grad(self, n_start: int) -> State:
+        """dJ/d(initial history rows [0, n_start)) from the last adjoint_backward."""
+        L = self.L
+        arrs = [np.zeros(n_start), np.zeros(n_start), np.empty(n_start * L), np.empty(n_start * L),
+                np.empty(n_start * L), np.empty(n_start * L), np.empty(n_start), np.empty(n_start)]
+        sc = _lib.StateC(n_start, *[_lib.ptr(x) for x in arrs])
+        _lib.check(_lib.lib().dyn_adjoint_history_grad(self._h, C.byref(sc)), "dyn_adjoint_history_grad")
+        return State(*arrs)
+
     def sparsifyNscale(self, threshold: float, variant: str = "gpu") -> int:
         v = C.c_size_t()
         _lib.check(_lib.lib().dyn_sparsify(self._h, threshold, SPARSIFY[variant], C.byref(v)), "dyn_sparsify")

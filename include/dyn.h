@@ -343,6 +343,50 @@ dyn_status dyn_batch_tune(void* batch, int reps, int* threads, int* targets, int
  * current stage of every running quench (the kernel is idempotent). */
 dyn_status dyn_batch_profile(void* batch, int reps, float* ms_gather);
 
+/* ------------------------------------------------------ discrete adjoint */
+/* No counterpart in the reference.  Gradients of a final-time objective
+ * with respect to the bath temperature Gamma and the mixing coupling lambda,
+ * by a hand-written discrete adjoint of the FP64 RK-stepped pipeline
+ * (interpolation, convolutions, RHS, r(t), RK stages) on a fixed step
+ * schedule.  The history is append-only, so the state before each step is a
+ * prefix of the final history: the reverse sweep recomputes one step's
+ * stages at a time from it and keeps no other checkpoint.  RK54 and
+ * SSPRK(10,4) steps only; FP64 contexts only. */
+typedef struct {
+    double w_energy;          /* weight of E(t_f) */
+    double w_r;               /* weight of r(t_f) */
+    const double* c_K;        /* [len] weights on C(t_f, theta_j t_f) of the final row, or NULL
+                                 (C(t_f, t_f/2): interpolation weights at theta = 1/2) */
+    const double* c_R;        /* [len] weights on R(t_f, theta_j t_f), or NULL */
+    const double* c_dK;       /* [len] weights on the final row's dQK, or NULL */
+    const double* c_dR;       /* [len] weights on the final row's dQR, or NULL */
+    double w_dr;              /* weight of the final row's drvec */
+} dyn_adjoint_objective;
+
+typedef struct {
+    double ms_forward;        /* wall time of the recorded forward steps */
+    double ms_backward;       /* wall time of the reverse sweep (recompute included) */
+    size_t device_bytes;      /* device memory the reverse sweep holds (cotangents, snapshot, scratch) */
+    int steps;
+    long long recompute_mismatch;  /* elements where a recomputed row differed from the forward's (0) */
+} dyn_adjoint_stats;
+
+/* dyn_run (no rollback) that records the step schedule it took (dt, method
+ * per step) for the reverse sweep; with p->dt_schedule it replays that
+ * schedule.  Gradients include the t=0 state's dependence on Gamma and
+ * lambda when the run starts from dyn_state_init's single row. */
+dyn_status dyn_adjoint_forward(void* ctx, const dyn_run_params* p, dyn_step_result* last);
+/* Reverse sweep of the recorded forward: grad[0] = dJ/dGamma, grad[1] =
+ * dJ/dlambda for J = w_energy E(t_f) + sum_j c_K[j] C(t_f, theta_j t_f) +
+ * w_r r(t_f) (+ the other final-row terms of the objective).  Leaves the history as the forward left it, so several
+ * objectives can be differentiated in turn. */
+dyn_status dyn_adjoint_backward(void* ctx, const dyn_adjoint_objective* obj, double* grad, dyn_adjoint_stats* stats);
+/* After dyn_adjoint_backward: dJ/d(history the recorded forward started
+ * from), rows [0, n_start) in dyn_state layout (t1grid, delta_t_ratio
+ * untouched).  The t=0 row's dependence on Gamma and lambda is already in
+ * grad; these are the sensitivities to an uploaded initial history. */
+dyn_status dyn_adjoint_history_grad(void* ctx, dyn_state* grad);
+
 /* ------------------------------------------------------------ tables */
 /* `RG-Evo grid -L len -M Tmax -s spline_order -m poly -o interp_order
  * -a alpha -D delta` (grid_cli.cpp:35-258) without the files: fills the
