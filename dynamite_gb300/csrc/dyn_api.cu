@@ -7,6 +7,7 @@
 // size L or L^2 lives on the device.  One RK step is one H2D copy of the
 // stage descriptors, 2 kernels per stage, and one D2H copy of the step result,
 // optionally replayed as a CUDA graph.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -92,7 +93,7 @@ struct Ctx {
 
     void release_adjoint() {
         void* ab[] = {ad.HKR, ad.HdKR, ad.Hr, ad.Hdr, ad.Gsave, ad.Dsave, ad.rsave, ad.drsave, ad.Psave, ad.hbar,
-                      ad.g0bar, ad.Gbar, ad.Dbar, ad.abar, ad.lbar_part, ad.sc, ad_ck, snap_KR, snap_dKR, snap_time};
+                      ad.g0bar, ad.Gbar, ad.Dbar, ad.abar, ad.lbar_part, ad.abarA, ad.sc, ad.b2pk, ad.b2rank, ad.rec, ad.lrW, ad.lrS, ad.lrC, ad_ck, snap_KR, snap_dKR, snap_time};
         for (void* b : ab) if (b) cudaFree(b);
         std::memset(&ad, 0, sizeof ad);
         ad_ck = nullptr;
@@ -368,13 +369,62 @@ struct Ctx {
             (s = dalloc(&ad.Dsave, (size_t)SMAX * Lz)) || (s = dalloc(&ad.rsave, SMAX)) || (s = dalloc(&ad.drsave, SMAX)) ||
             (s = dalloc(&ad.Psave, (size_t)SMAX * Lz)) || (s = dalloc(&ad.hbar, (size_t)SMAX * Lz)) ||
             (s = dalloc(&ad.g0bar, Lz)) || (s = dalloc(&ad.Gbar, Lz)) || (s = dalloc(&ad.Dbar, Lz)) ||
-            (s = dalloc(&ad.abar, 8 * Lz)) || (s = dalloc(&ad.lbar_part, Lz * Lz)) || (s = dalloc(&ad.sc, 16)) ||
+            (s = dalloc(&ad.abar, 8 * Lz)) || (s = dalloc(&ad.lbar_part, Lz * Lz)) || (s = dalloc(&ad.abarA, 2 * Lz * Lz)) || (s = dalloc(&ad.sc, 16)) ||
+            (s = dalloc(&ad.b2pk, Lz * Lz)) || (s = dalloc(&ad.b2rank, Lz * Lz)) ||
+            (s = dalloc(&ad.rec, (size_t)SMAX * Lz * Lz)) || (s = dalloc(&ad.lrW, 2 * Lz * Lz * (size_t)d.m)) ||
+            (s = dalloc(&ad.lrS, 2 * Lz * Lz * (size_t)d.m)) || (s = dalloc(&ad.lrC, Lz * (Lz + 1))) ||
             (s = dalloc(&ad_ck, 4 * Lz)) || (s = dalloc(&snap_KR, cap * Lz)) || (s = dalloc(&snap_dKR, cap * Lz)) ||
             (s = dalloc(&snap_time, 5 * cap))) {
             release_adjoint();
             return s;
         }
-        CK(adj_targets_smem_attr(L));
+        CK(adj_targets_smem_attr(L, d.m));
+        {
+            // static orders of the transposed gathers (the tables never change)
+            const size_t L2 = Lz * Lz;
+            std::vector<double> ph(L2);
+            std::vector<long long> iA(2 * L2), iB(L2);
+            CK(cudaMemcpy(ph.data(), d.phi2, L2 * sizeof(double), cudaMemcpyDeviceToHost));
+            std::vector<int> i32(L2);
+            for (int t = 0; t < 3; ++t) {
+                CK(cudaMemcpy(i32.data(), t == 0 ? d.iA1 : t == 1 ? d.iA2 : d.iB2, L2 * sizeof(int),
+                              cudaMemcpyDeviceToHost));
+                long long* dst = t < 2 ? iA.data() + t * L2 : iB.data();
+                for (size_t e = 0; e < L2; ++e) dst[e] = i32[e];
+            }
+            std::vector<int> ord(L2), rank(L2);
+            for (size_t e = 0; e < L2; ++e) ord[e] = (int)e;
+            std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+                return iB[x] != iB[y] ? iB[x] < iB[y] : ph[x] < ph[y];
+            });
+            for (size_t q = 0; q < L2; ++q) rank[ord[q]] = (int)q;
+            CK(cudaMemcpy(ad.b2rank, rank.data(), L2 * sizeof(int), cudaMemcpyHostToDevice));
+            // A1/A2 of each row as a column-sorted sparse matrix (counting sort by column)
+            const size_t mz = d.m, E = 2 * Lz * mz;
+            std::vector<double> wA(2 * L2 * mz), lw(Lz * E);
+            CK(cudaMemcpy(wA.data(), d.wA1, L2 * mz * sizeof(double), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(wA.data() + L2 * mz, d.wA2, L2 * mz * sizeof(double), cudaMemcpyDeviceToHost));
+            std::vector<int> ls(Lz * E), lc(Lz * (Lz + 1));
+            for (size_t i = 0; i < Lz; ++i) {
+                int* cs = lc.data() + i * (Lz + 1);
+                std::fill(cs, cs + Lz + 1, 0);
+                for (int t = 0; t < 2; ++t)
+                    for (size_t j = 0; j < Lz; ++j)
+                        for (size_t dd = 0; dd < mz; ++dd) ++cs[iA[t * L2 + i * Lz + j] + dd + 1];
+                for (size_t k = 0; k < Lz; ++k) cs[k + 1] += cs[k];
+                std::vector<int> fill(cs, cs + Lz);
+                for (int t = 0; t < 2; ++t)
+                    for (size_t j = 0; j < Lz; ++j)
+                        for (size_t dd = 0; dd < mz; ++dd) {
+                            const size_t col = iA[t * L2 + i * Lz + j] + dd, p = i * E + fill[col]++;
+                            lw[p] = wA[t * L2 * mz + (i * Lz + j) * mz + dd];
+                            ls[p] = (int)(2 * j + t);
+                        }
+            }
+            CK(cudaMemcpy(ad.lrW, lw.data(), Lz * E * sizeof(double), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(ad.lrS, ls.data(), Lz * E * sizeof(int), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(ad.lrC, lc.data(), Lz * (Lz + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        }
         ad_cap = cap;
         return DYN_OK;
     }
@@ -382,7 +432,9 @@ struct Ctx {
     size_t adjoint_bytes() const {
         const size_t Lz = L;
         return (cap * Lz * 2 * sizeof(double2)) * 2 + cap * 2 * sizeof(double) + 5 * cap * sizeof(double) +
-               (size_t)SMAX * Lz * (3 * sizeof(double2) + sizeof(double)) + Lz * Lz * sizeof(double2) +
+               (size_t)SMAX * Lz * (3 * sizeof(double2) + sizeof(double)) + 3 * Lz * Lz * sizeof(double2) +
+               Lz * Lz * (sizeof(AdjDev::B2Packet) + sizeof(int) + SMAX * sizeof(GatherRec)) +
+               2 * Lz * Lz * (size_t)d.m * (sizeof(double) + sizeof(int)) + Lz * (Lz + 1) * sizeof(int) +
                Lz * (3 * sizeof(double2) + 9 * sizeof(double)) + 2 * SMAX * sizeof(double) + 16 * sizeof(double);
     }
 
@@ -404,7 +456,9 @@ struct Ctx {
         CK(cudaEventRecord(stages_copied, st));
         for (int k = 0; k < S; ++k) {
             CK(cudaMemcpyAsync(ad.Psave + k * Lz, d.posB1x, Lz * sizeof(double), cudaMemcpyDeviceToDevice, st));
-            CK(launch_stage(d, k, st));
+            DevCtx dr = d;
+            dr.rec = ad.rec + (size_t)k * Lz * Lz;  // k_main records its gathers for the reverse stage
+            CK(launch_stage(dr, k, st));
             CK(cudaMemcpyAsync(ad.Gsave + k * Lz, d.KR + n0 * Lz, Lz * sizeof(double2), cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(ad.Dsave + k * Lz, d.dKR + n0 * Lz, Lz * sizeof(double2), cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(ad.rsave + k, d.rvec + n0, sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1079,6 +1133,7 @@ dyn_status dyn_adjoint_backward(void* p, const dyn_adjoint_objective* obj, doubl
         return fail(DYN_ERR_STATE, "no recorded forward: call dyn_adjoint_forward (the history changed since)");
     for (int m : c->adj_method)
         if (m != DYN_RK54 && m != DYN_SSPRK104) return fail(DYN_ERR_UNSUPPORTED, "adjoint of SERK2 steps is not built");
+    if (c->L > 4096) return fail(DYN_ERR_UNSUPPORTED, "len <= 4096");
     dyn_status s = c->adjoint_alloc();
     if (s) return s;
     const auto t0 = std::chrono::steady_clock::now();

@@ -142,6 +142,7 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
                         b2.x = e0 * S0.x + x2 * S1.x + e2 * D1.x;
                         b2.y = e0 * S0.y + x2 * S1.y + e2 * D1.y;
                     }
+                    if (c.rec) c.rec[ij] = GatherRec{a1, a2, b1, b2, x, (int)X, 0};
                 }
             } else {
                 a1 = a2 = b1 = b2 = fill;

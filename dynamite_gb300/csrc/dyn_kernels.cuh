@@ -47,6 +47,16 @@ struct Slots {
     double res_err, res_energy, res_r, res_qk0, res_dr;
 };
 
+// Per-target gathered values of one stage, recorded by k_main when
+// DevCtx::rec is set (the adjoint's recompute) and read back by k_adj_targets
+// instead of gathering again.
+struct GatherRec {
+    double2 a1, a2, b1, b2;  // (QK, QR) at the A1, A2, B1, B2 points
+    double x;                // B2 position fraction
+    int X;                   // B2 row (clamped)
+    int pad;
+};
+
 struct DevCtx {
     int L, m, nch, search, kpt, tpb;
     int mixed;             // 1: FP32 gathers/convolutions (dyn_mixed.cu)
@@ -95,6 +105,7 @@ struct DevCtx {
     // materialized interpolation (dyn_interpolate)
     double* ip;            // [16][L*L]
     double* rint;          // [L]
+    GatherRec* rec;        // [L*L] gathered values of this stage, or null
 };
 
 // Adjoint state of the FP64 path (dyn_adjoint.cu): cotangents of the
@@ -115,7 +126,24 @@ struct AdjDev {
     double2* Dbar;     // [L]
     double* abar;      // [L][8] cotangents of the eight memory-integral rows
     double2* lbar_part;  // [L][L] per-target-row last-row stencil cotangents
+    double2* abarA;      // [L*L][2] cotangents of each target's A1 and A2 gathers
     double* sc;        // scalars: rho, delta, DR, Gamma, lambda
+    // B2 cotangents of one stage, one packet per target, stored in the static
+    // (iB2, phi2) order: the targets that share a B2 stencil row (X, iB2) in a
+    // stage then sit next to each other (X is monotonic in phi2).
+    struct B2Packet {
+        int ij, X;
+        double x, gK, gR;
+    };
+    B2Packet* b2pk;      // [L*L]
+    int* b2rank;         // [L*L] packet slot of target ij
+    GatherRec* rec;      // [SMAX][L*L] gathered values of each stage of the recomputed step
+    // A1 and A2 gathers of each target row as one column-sorted sparse
+    // matrix onto the last row (static): entry p of row i adds
+    // lrW[p] * (cotangent 2j+t of the row) to column k for lrC[k] <= p < lrC[k+1]
+    double* lrW;         // [L][2*L*m]
+    int* lrS;            // [L][2*L*m] source 2j+t
+    int* lrC;            // [L][L+1] column starts
 };
 struct AdjModel {
     int p, p2;
@@ -199,6 +227,6 @@ cudaError_t launch_adj_step(const DevCtx& c, const AdjDev& a, const AdjModel& am
 cudaError_t launch_adj_initial(const AdjDev& a, const AdjModel& am, cudaStream_t st);
 cudaError_t launch_adj_verify(const DevCtx& c, const AdjDev& a, const double2* snapKR, const double2* snapdKR,
                               const double* snapr, const double* snapdr, int n0, cudaStream_t st);
-cudaError_t adj_targets_smem_attr(int L);
+cudaError_t adj_targets_smem_attr(int L, int m);
 
 }  // namespace dyn
