@@ -465,33 +465,48 @@ __global__ void __launch_bounds__(256) k_adj_lastrow(const DevCtx c, const AdjDe
     const StageDev& sp = c.stages[s];
     if (!(sp.T > 0.0)) return;
     const int L = c.L, i = blockIdx.x, E = 2 * L * c.m;
-    extern __shared__ double2 s_acc[];  // [L] row sums, [2L] the row's A1/A2 cotangents (2j+t)
+    extern __shared__ double2 s_acc[];  // [L] row sums, [2L] the row's A1/A2 cotangents (2j+t), int [L+1] column starts
     double2* s_cb = s_acc + L;
+    int* s_cs = (int*)(s_acc + 3 * L);
     const size_t row = (size_t)i * L;
+    const int* cs = a.lrC + (size_t)i * (L + 1);
     for (int k = threadIdx.x; k < L; k += blockDim.x) s_acc[k] = make_double2(0.0, 0.0);
     for (int k = threadIdx.x; k < 2 * L; k += blockDim.x) s_cb[k] = a.abarA[2 * row + k];
+    for (int k = threadIdx.x; k <= L; k += blockDim.x) s_cs[k] = __ldg(cs + k);
     __syncthreads();
     const int per = (E + blockDim.x - 1) / blockDim.x;
     const int p0 = threadIdx.x * per, p1 = min(p0 + per, E);
     if (p0 < p1) {
-        const int* cs = a.lrC + (size_t)i * (L + 1);
         const double* w = a.lrW + (size_t)i * E;
         const int* src = a.lrS + (size_t)i * E;
         int lo = 0, hi = L;  // column of entry p0: the last k with cs[k] <= p0
-        while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (__ldg(cs + mid) <= p0) lo = mid; else hi = mid; }
-        int k = lo, kend = __ldg(cs + k + 1);
+        while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (s_cs[mid] <= p0) lo = mid; else hi = mid; }
+        int k = lo, kend = s_cs[k + 1];
         double ax = 0.0, ay = 0.0;
-        for (int p = p0; p < p1; ++p) {
-            if (p >= kend) {
-                atomicAdd(&s_acc[k].x, ax);
-                atomicAdd(&s_acc[k].y, ay);
-                ax = ay = 0.0;
-                do { ++k; kend = __ldg(cs + k + 1); } while (p >= kend);
+        constexpr int B = 8;  // entries loaded ahead
+        for (int pb = p0; pb < p1; pb += B) {
+            double u[B];
+            int si[B];
+#pragma unroll
+            for (int q = 0; q < B; ++q) {
+                const bool in = pb + q < p1;
+                u[q] = in ? __ldg(w + pb + q) : 0.0;
+                si[q] = in ? __ldg(src + pb + q) : 0;
             }
-            const double u = __ldg(w + p);
-            const double2 v = s_cb[__ldg(src + p)];
-            ax = fma(u, v.x, ax);
-            ay = fma(u, v.y, ay);
+#pragma unroll
+            for (int q = 0; q < B; ++q) {
+                const int p = pb + q;
+                if (p >= p1) break;
+                if (p >= kend) {
+                    atomicAdd(&s_acc[k].x, ax);
+                    atomicAdd(&s_acc[k].y, ay);
+                    ax = ay = 0.0;
+                    do { ++k; kend = s_cs[k + 1]; } while (p >= kend);
+                }
+                const double2 v = s_cb[si[q]];
+                ax = fma(u[q], v.x, ax);
+                ay = fma(u[q], v.y, ay);
+            }
         }
         atomicAdd(&s_acc[k].x, ax);
         atomicAdd(&s_acc[k].y, ay);
@@ -720,8 +735,9 @@ cudaError_t launch_adj_seed(const DevCtx& c, const AdjDev& a, const AdjModel& am
     return cudaGetLastError();
 }
 
-// k_adj_lastrow's shared memory: row sums and the row's A1/A2 cotangents
-size_t lastrow_smem(int L, int) { return 3 * (size_t)L * sizeof(double2); }
+// k_adj_lastrow's shared memory: row sums, the row's A1/A2 cotangents and
+// the column starts
+size_t lastrow_smem(int L, int) { return 3 * (size_t)L * sizeof(double2) + (size_t)(L + 1) * sizeof(int); }
 
 template <int P, int P2>
 cudaError_t launch_targets_pp(const DevCtx& c, const AdjDev& a, const AdjModel& am, int s,
