@@ -13,7 +13,11 @@ as each quench's controller chooses); value = RK steps completed / time.
 Beside it, on the same grid: the plain FP64 form of one quench (lam=0.5,
 T=0.6) after the same setup, its stage kernels and FP64 roofline; the
 single-quench mixed form on that state; the reference CPU path (oracle/
-restatement) on the host cores.
+restatement) on the host cores.  Then the mixed-L batch (64 quenches with
+grid lengths from {256, 512, 1024} and stopping times log-uniform on
+[1e4, 1e7]) and the FP64 adjoint (L=512, lam=0.5, T=0.6, 5000 steps:
+gradients of E, C(t, t/2) and r in T and lam against central differences,
+backward/forward time, device memory).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -54,6 +58,9 @@ def parse():
     ap.add_argument("--no-mixed", dest="mixed", action="store_false", help="skip the single-quench mixed measurement")
     ap.add_argument("--quenches", type=int, default=64)
     ap.add_argument("--tune", action="store_true", help="autotune the batched gather tile before timing")
+    ap.add_argument("--config4-setup", type=int, default=1000,
+                    help="untimed steps of every quench of the mixed-L batch before its timed ticks (0: skip it)")
+    ap.add_argument("--adjoint-steps", type=int, default=5000, help="FP64 steps of the adjoint measurement (0: skip)")
     return ap.parse_args()
 
 
@@ -279,6 +286,99 @@ def _batch_alg_bytes(L: int, m: int, n: float) -> float:
     return 3 * L * L * (4 * m + 4) + 8 * L * L + 16 * L * n + 64 * L
 
 
+def _config4(D, torch, args, dev, stream):
+    """The mixed-L batch: 64 quenches, temperatures uniform on [0.4, 1.0], lambda cycling
+    0.3/0.5/0.7, grid length from {256, 512, 1024} and stopping time log-uniform on [1e4, 1e7]
+    drawn from mt19937_64 (fixed seed), mixed precision.  Every quench takes `config4_setup`
+    steps untimed from t=0, then `steps` ticks are timed; value = RK steps completed / time."""
+    from dynamite_gb300.batch import config4_quenches
+    cap = args.config4_setup + args.steps + 64
+    lengths, qs = config4_quenches(n=args.quenches, capacity=cap, max_steps=args.config4_setup)
+    grids = [D.grid.generate(L) for L in lengths]
+    bt = D.Batch(grids, qs, ticks_per_launch=32, device=dev, stream=stream.cuda_stream)
+    bt.run(10 ** 9)
+    for q in range(len(qs)):
+        bt.set_limits(q, t_stop=qs[q].t_stop, max_steps=10 ** 12)
+    bt.run(args.warmup)
+    steps0 = bt.total_steps()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    bt.enqueue(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    bt.sync()
+    t = e0.elapsed_time(e1) / 1e3
+    steps = bt.total_steps() - steps0
+    infos = bt.infos()
+    per_L = {str(L): sum(1 for q in qs if grids[q.grid].L == L) for L in lengths}
+    out = {"value": steps / t, "unit": UNIT, "ticks": args.steps, "rk_steps_timed": steps,
+           "ms_per_tick": 1e3 * t / args.steps, "quenches_per_L": per_L,
+           "t_stop_range": [min(q.t_stop for q in qs), max(q.t_stop for q in qs)],
+           "t_reached_range": [min(i["t"] for i in infos), max(i["t"] for i in infos)],
+           "setup_steps": args.config4_setup,
+           "note": "timed window of the job after the untimed setup; no quench reaches its stopping time "
+                   "inside the window"}
+    bt.close()
+    return out
+
+
+def _adjoint(D, torch, args, dev):
+    """Discrete adjoint of the FP64 path: mixed p-spin lam=0.5, T=0.6, L, `adjoint_steps` steps
+    from t=0.  Gradients of E(t_f), C(t_f, t_f/2) and r(t_f) in (T, lam) by three reverse sweeps
+    over the recorded schedule, each checked against central differences (h=1e-5 relative) of
+    the FP64 forward on the same schedule; backward/forward wall-time ratio and the device
+    memory the forward+adjoint held."""
+    N = args.adjoint_steps
+    grid = D.grid.generate(args.L)
+    kw = model_kw()
+    free0 = torch.cuda.mem_get_info(dev)[0]
+    s = D.Simulation(grid, D.Model(**kw), device=dev, history_capacity=N + 16)
+    s.init()
+    fw = s.adjoint_forward(N)
+    sched = (fw["dt"], fw["method"])
+    cK = D.grid.lagrange_weights(grid.theta, 0.5)
+    gE, st = s.adjoint_backward(w_energy=1.0)
+    gC, stC = s.adjoint_backward(c_K=cK)
+    gR, stR = s.adjoint_backward(w_r=1.0)
+    used = free0 - torch.cuda.mem_get_info(dev)[0]
+    s.close()
+
+    def objectives(sim):
+        last = sim.download().QK[-args.L:]
+        return np.array([sim.energy(), float(cK @ last), float(sim.download().rvec[-1])])
+
+    H = 1e-5
+    fd = {}
+    for name, base in (("Gamma", kw["Gamma"]), ("lam", kw["lam"])):
+        vals = []
+        for sg in (+1, -1):
+            k2 = dict(kw)
+            k2[name] = base * (1 + sg * H)
+            t = D.Simulation(grid, D.Model(**k2), device=dev, history_capacity=N + 16)
+            t.init()
+            t.run(N, schedule=sched)
+            vals.append(objectives(t))
+            t.close()
+        fd[name] = (vals[0] - vals[1]) / (2 * H * base)
+    adj = {"E": gE, "C": gC, "r": gR}
+    checks = {}
+    for k, obj in enumerate(("E", "C", "r")):
+        for j, name in enumerate(("Gamma", "lam")):
+            a, f = float(adj[obj][j]), float(fd[name][k])
+            checks[f"d{obj}/d{'T' if name == 'Gamma' else 'lam'}"] = {
+                "adjoint": a, "fd": f, "rel_err": abs(a - f) / max(abs(f), 1e-300)}
+    ratios = [x["ms_backward"] / x["ms_forward"] for x in (st, stC, stR)]
+    return {"L": args.L, "steps": N, "t_final": float(fw["t"][-1]), "ms_forward": st["ms_forward"],
+            "ms_backward": st["ms_backward"], "bwd_fwd_ratio": ratios[0], "bwd_fwd_ratio_all": ratios,
+            "peak_device_bytes": int(used), "adjoint_workspace_bytes": st["device_bytes"],
+            "recompute_mismatch": st["recompute_mismatch"] + stC["recompute_mismatch"] + stR["recompute_mismatch"],
+            "headline_gradients": {k: checks[k] for k in ("dE/dT", "dC/dlam", "dr/dT")},
+            "all_gradients": checks,
+            "checkpointing": "append-only history: the state before step k is the first n_k rows of the final "
+                             "history, so every step is recomputed from its prefix with no stored checkpoint"}
+
+
 def run_ours(args):
     import torch
 
@@ -359,6 +459,8 @@ def run_ours(args):
 
     if rank != 0:
         return
+    config4 = _config4(D, torch, args, dev, stream) if args.config4_setup > 0 else None
+    adjoint = _adjoint(D, torch, args, dev) if args.adjoint_steps > 0 else None
     # ---- roofline of the dominant kernel: the batched gather, timed live on its stream
     ms_gather = bt.profile(reps=10)
     L, m = args.L, grid.depth
@@ -395,6 +497,8 @@ def run_ours(args):
                                      "flop_per_launch": fp64_flop, "kernel": "k_main (FP64 fused gather)",
                                      "peak_source": "measured (dyn_probe_fp64, same run)"}),
         "mixed_single": mixed,
+        "config4_mixed_L": config4,
+        "adjoint": adjoint,
         "e2e": {"value": e2e_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h_tick, "note": "per tick; dyn_batch_run of 32 ticks + newest rows"},
         "gpu_launches": int(2 * args.steps),
