@@ -11,9 +11,20 @@ the staggered derivatives (t_k - t_{k-1}) d/dt C(t, theta_j t) at t_{k-1}
     python -m dynamite_gb300.microbench --form mixed --L 512 --rows 4096 --reps 20
     python -m dynamite_gb300.microbench --form batch --L 512 --rows 1500 --quenches 64 --reps 3
 
+    python -m dynamite_gb300.microbench --form adjoint --L 512 --steps 20
+    python -m dynamite_gb300.microbench --form mixed_error --L 1024 --steps 5000
+
 `fp64` / `mixed` time the single-quench gather+convolution kernel and the
 epilogue (one right-hand side at t = t_{n-1}); `batch` times the batched
-gather over `quenches` copies of the history.  Prints one JSON line.
+gather over `quenches` copies of the history; `adjoint` runs the FP64
+forward of the mixed p-spin quench (lam=0.5, T=0.6) from t=0 for `steps`
+steps with its schedule recorded, then one reverse sweep for d E(t_f) /
+d(T, lam), and reports both wall times; `mixed_error` runs the FP64 form of
+that quench for `steps` steps and replays its step schedule in the mixed
+form, then reports the relative error of the mixed run per observable:
+energy over the run, r(t), C and R over the whole history, the equal-time
+C(t, t), and at the final time t_f C(t_f/2, t_f) and R(t_f, t_f/2).
+Prints one JSON line.
 """
 from __future__ import annotations
 
@@ -41,9 +52,40 @@ def synthetic_history(grid: Grid, n: int, T: float = 0.6, t_lo: float = 1e-5, t_
     return State(t, dtr, QK.ravel(), QR.ravel(), dQK.ravel(), dQR.ravel(), np.ones(n), np.zeros(n))
 
 
+def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5) -> dict:
+    """Mixed form against the FP64 form on the FP64 run's step schedule (see module doc)."""
+    from .grid import lagrange_weights
+    from .simulation import Model, Simulation
+    L = grid.L
+    m = Model(p=3, p2=4, lam=lam, Gamma=T)
+    a = Simulation(grid, m, history_capacity=nsteps + 64)
+    b = Simulation(grid, m, precision="mixed", history_capacity=nsteps + 64)
+    a.init()
+    b.init()
+    ta = a.run(nsteps)
+    tb = b.run(nsteps, schedule=(ta["dt"], ta["method"]))
+    sa, sb = a.download(), b.download()
+    a.close()
+    b.close()
+    QA, QB = sa.QK.reshape(-1, L), sb.QK.reshape(-1, L)
+    RA, RB = sa.QR.reshape(-1, L), sb.QR.reshape(-1, L)
+    t = sa.t1grid
+    w = lagrange_weights(grid.theta, 0.5)
+    # C(t_f/2, t_f) = C(t_f, theta t_f) at theta = 1/2 (C symmetric), R(t_f, t_f/2) likewise
+    c_a, c_b = float(w @ QA[-1]), float(w @ QB[-1])
+    r_a, r_b = float(w @ RA[-1]), float(w @ RB[-1])
+    rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+    return {"form": "mixed_error", "L": L, "steps": nsteps, "t_final": float(t[-1]), "T": T, "lam": lam,
+            "time_grid_identical": bool(np.array_equal(sa.t1grid, sb.t1grid)),
+            "energy": rel(tb["energy"], ta["energy"]), "r": rel(sb.rvec, sa.rvec), "C_history": rel(QB, QA),
+            "R_history": rel(RB, RA), "C_equal_time_abs": float(np.max(np.abs(QB[:, -1] - QA[:, -1]))),
+            "C_tf_half_tf": abs(c_b - c_a) / abs(c_a), "R_tf_tf_half": abs(r_b - r_a) / abs(r_a)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--form", choices=["fp64", "mixed", "batch"], default="batch")
+    ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error"], default="batch")
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--L", type=int, default=512)
     ap.add_argument("--rows", type=int, default=4096)
     ap.add_argument("--quenches", type=int, default=16)
@@ -57,6 +99,18 @@ def main(argv=None):
     from .simulation import Model, Simulation
 
     grid = G.generate(a.L)
+    if a.form == "adjoint":
+        s = Simulation(grid, Model(p=3, p2=4, lam=0.5, Gamma=a.T), history_capacity=a.steps + 16)
+        s.init()
+        fw = s.adjoint_forward(a.steps)
+        g, stats = s.adjoint_backward(w_energy=1.0)
+        s.close()
+        print(json.dumps({"form": "adjoint", "L": a.L, "steps": a.steps, "t_final": float(fw["t"][-1]),
+                          "dE_dT": float(g[0]), "dE_dlam": float(g[1]), **stats}))
+        return
+    if a.form == "mixed_error":
+        print(json.dumps(mixed_error(grid, a.steps, a.T)))
+        return
     st = synthetic_history(grid, a.rows, a.T)
     t = st.t1grid
     out = {"form": a.form, "L": a.L, "rows": a.rows}
