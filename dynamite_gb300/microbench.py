@@ -52,8 +52,10 @@ def synthetic_history(grid: Grid, n: int, T: float = 0.6, t_lo: float = 1e-5, t_
     return State(t, dtr, QK.ravel(), QR.ravel(), dQK.ravel(), dQR.ravel(), np.ones(n), np.zeros(n))
 
 
-def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5) -> dict:
-    """Mixed form against the FP64 form on the FP64 run's step schedule (see module doc)."""
+def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5, tmax: float = 0.0) -> dict:
+    """Mixed form against the FP64 form on the FP64 run's step schedule (see module doc);
+    with tmax > 0 the FP64 run stops at t >= tmax (nsteps is then a cap)."""
+    import time
     from .grid import lagrange_weights
     from .simulation import Model, Simulation
     L = grid.L
@@ -62,8 +64,14 @@ def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5) -> di
     b = Simulation(grid, m, precision="mixed", history_capacity=nsteps + 64)
     a.init()
     b.init()
-    ta = a.run(nsteps)
-    tb = b.run(nsteps, schedule=(ta["dt"], ta["method"]))
+    t0 = time.perf_counter()
+    ta = a.run(nsteps, tmax=tmax)
+    t1 = time.perf_counter()
+    done = int(np.count_nonzero(ta["dt"]))
+    ta = {k: v[:done] for k, v in ta.items()}
+    tb = b.run(done, schedule=(ta["dt"], ta["method"]))
+    t2 = time.perf_counter()
+    nsteps = done
     sa, sb = a.download(), b.download()
     a.close()
     b.close()
@@ -76,6 +84,7 @@ def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5) -> di
     r_a, r_b = float(w @ RA[-1]), float(w @ RB[-1])
     rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
     return {"form": "mixed_error", "L": L, "steps": nsteps, "t_final": float(t[-1]), "T": T, "lam": lam,
+            "history_rows": int(t.size), "s_fp64": t1 - t0, "s_mixed": t2 - t1,
             "time_grid_identical": bool(np.array_equal(sa.t1grid, sb.t1grid)),
             "energy": rel(tb["energy"], ta["energy"]), "r": rel(sb.rvec, sa.rvec), "C_history": rel(QB, QA),
             "R_history": rel(RB, RA), "C_equal_time_abs": float(np.max(np.abs(QB[:, -1] - QA[:, -1]))),
@@ -86,6 +95,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error"], default="batch")
     ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--tmax", type=float, default=0.0, help="mixed_error: run the FP64 form to t >= tmax")
     ap.add_argument("--L", type=int, default=512)
     ap.add_argument("--rows", type=int, default=4096)
     ap.add_argument("--quenches", type=int, default=16)
@@ -109,7 +119,7 @@ def main(argv=None):
                           "dE_dT": float(g[0]), "dE_dlam": float(g[1]), **stats}))
         return
     if a.form == "mixed_error":
-        print(json.dumps(mixed_error(grid, a.steps, a.T)))
+        print(json.dumps(mixed_error(grid, a.steps, a.T, tmax=a.tmax)))
         return
     st = synthetic_history(grid, a.rows, a.T)
     t = st.t1grid
