@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(64) k_adj_targets(const DevCtx c, const AdjDev
         add2(a.HKR + (size_t)F * L + j, bc1 * b1Kb, bc1 * b1Rb);
         add2(a.HdKR + (size_t)F * L + j, -bc2 * b1Kb, -bc2 * b1Rb);
         if (cubic1) add2(a.HdKR + (size_t)(F + 1) * L + j, -bc3 * b1Kb, -bc3 * b1Rb);
-        // B2 transposed by k_adj_b2seg from the packet in static order
+        // B2 transposed by k_adj_b2ser from the packet in static order
         a.b2pk[__ldg(a.b2rank + ij)] = AdjDev::B2Packet{(int)ij, X, x, b2Kb, b2Rb};
     }
     lam = warp_sum(lam);

@@ -588,9 +588,10 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
             if ((s = bt->alloc(&gd.iA[k], L2)) || (s = bt->alloc(&gd.wf[k], planes * L2))) { delete bt; return s; }
             BUP(gd.iA[k], i32[k].data(), L2 * sizeof(int));
             // the layout of k_weights_tapmajor (dyn_mixed.cu)
-            for (size_t e = 0; e < L2; ++e)
+            for (size_t tg = 0; tg < L2; ++tg)
                 for (size_t d = 0; d < m; d += 2)
-                    wt[(d >> 1) * L2 + e] = make_float2((float)w[k][e * m + d], d + 1 < m ? (float)w[k][e * m + d + 1] : 0.0f);
+                    wt[(d >> 1) * L2 + tg] =
+                        make_float2((float)w[k][tg * m + d], d + 1 < m ? (float)w[k][tg * m + d + 1] : 0.0f);
             BUP(gd.wf[k], wt.data(), planes * L2 * sizeof(float2));
         }
     }
