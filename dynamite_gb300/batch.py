@@ -9,6 +9,11 @@ in the mixed-precision arithmetic of `Simulation(precision="mixed")`.
     b.run(max_ticks=10_000)
     b.info(0)["t"], b.download(0).QK
 
+With `sparsify_every` > 0 every quench takes the reference driver's periodic
+sparsify (simulation_runner.cpp:148-237) after each loop that is a multiple
+of it: it pauses at that step's end and the host compacts its history between
+graph replays.
+
 `config4_quenches` draws the 64-quench workload (temperatures on [0.4, 1.0],
 lambda in {0.3, 0.5, 0.7}, grid length from {256, 512, 1024}, stopping times
 log-uniform on [1e4, 1e7]) from `mt19937_64` with a fixed seed.
@@ -22,9 +27,9 @@ import numpy as np
 
 from . import _lib
 from .grid import Grid
-from .simulation import SEARCH, State
+from .simulation import SEARCH, SPARSIFY, State
 
-STATUS = {0: "running", 1: "done", 2: "max_steps", 3: "full"}
+STATUS = {0: "running", 1: "done", 2: "max_steps", 3: "full", 4: "sparsify"}
 
 
 @dataclass
@@ -46,7 +51,8 @@ class Quench:
 class Batch:
     def __init__(self, grids: list[Grid], quenches: list[Quench], search: str = "binary", gpu_rollback: bool = False,
                  ticks_per_launch: int = 32, threads: int = 128, targets: int = 1, ctas_per_sm: int = 0,
-                 device: int = 0, stream: int | None = None):
+                 device: int = 0, stream: int | None = None, sparsify_every: int = 0, sparsify_sweeps: int = 1,
+                 sparsify_variant: str = "gpu"):
         self.grids = grids
         self.quenches = list(quenches)
         self._h = C.c_void_p()
@@ -64,7 +70,7 @@ class Batch:
             qs[k] = _lib.BatchQuench(q.grid, q.p, q.p2, q.lam, q.T0, q.Gamma, q.delta_t_min, q.delta_max, q.delta_t,
                                      q.t_stop, q.max_steps, q.capacity)
         cfg = _lib.BatchConfig(device, stream, SEARCH[search], int(gpu_rollback), ticks_per_launch, threads, targets,
-                               ctas_per_sm)
+                               ctas_per_sm, sparsify_every, sparsify_sweeps, SPARSIFY[sparsify_variant])
         _lib.check(_lib.lib().dyn_batch_create(C.byref(cfg), gs, len(grids), qs, len(quenches), C.byref(self._h)),
                    "dyn_batch_create")
         del keep  # the tables were copied to the device

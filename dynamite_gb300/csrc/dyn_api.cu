@@ -59,6 +59,7 @@ struct Ctx {
     std::vector<double> t1, dtr;
     size_t n = 0, cap = 0;
     dyn_controller ctl{};
+    int last_rollback_loop = -1000;  // loop of the last rollback (simulation_runner.cpp:53, :290)
     double specRad = 0.0;
     // pinned staging
     StageDev* stages_h = nullptr;
@@ -580,6 +581,66 @@ std::vector<double> serk_coeffs(int q) {
 
 }
 
+namespace dyn {
+// Keep list of one sparsify pass from the per-node flags (bit 1: evaluated,
+// bit 2: below the threshold, bit 4: kept by the GPU variant): the index logic
+// of each variant (sparsify_utils.cpp:14-97, .cu:38-113, .cu:154-290), the
+// derivative rows and their time rescaling (.cu:74-86, :230-265), and the new
+// t1grid / delta_t_ratio (.cpp:76-96, .cu:99-110).  False when variant 0
+// erases nothing (the reference leaves the state untouched).
+bool sparsify_indices(const unsigned char* fl, size_t n, int variant, const std::vector<double>& t1,
+                      const std::vector<double>& dtr, std::vector<int>& inds, std::vector<int>& indsD,
+                      std::vector<double>& tfac, std::vector<double>& t1n, std::vector<double>& dtrn) {
+    inds.clear();
+    bool erased = false;
+    if (variant == 0) {
+        inds.push_back(0);
+        for (size_t i = 2; i + 1 < n; ++i) {
+            if (fl[i] & 2) erased = true; else inds.push_back((int)i);
+        }
+        inds.push_back((int)n - 1);
+        if (!erased) return false;
+    } else if (variant == 1) {
+        int loop = 0;
+        inds.push_back(0);
+        for (size_t i = 2; i + 1 < n; ++i) {
+            if ((fl[i] & 2) && !erased) { erased = true; ++loop; }
+            else { erased = false; ++loop; inds.push_back(loop); }
+        }
+        inds.push_back((int)n - 2);
+        inds.push_back((int)n - 1);
+    } else {
+        for (size_t i = 0; i < n; ++i) if (!(fl[i] & 1) || (fl[i] & 4)) inds.push_back((int)i);
+    }
+    const int k = (int)inds.size();
+    indsD.assign(k, 0);
+    tfac.assign(k, 1.0);
+    if (variant == 0) {
+        indsD = inds;
+    } else {
+        for (int i = 0; i + 1 < k; ++i) indsD[i + 1] = inds[i] + 1;
+        for (int i = 1; i < k; ++i) {
+            const double num = t1[inds[i]] - t1[inds[i - 1]];
+            const double den = t1[indsD[i]] - t1[indsD[i] - 1];
+            tfac[i] = variant == 2 ? (den != 0.0 ? num / den : 1.0) : num / den;
+        }
+    }
+    t1n.assign(k, 0.0);
+    for (int i = 0; i < k; ++i) t1n[i] = t1[inds[i]];
+    if (variant == 0) {
+        dtrn.assign(k, 0.0);
+        for (int i = 0; i < k; ++i) dtrn[i] = dtr[inds[i]];
+    } else {
+        dtrn = dtr;
+        dtrn.resize(k);
+        std::vector<double> dg(k, 0.0);
+        for (int i = 1; i < k; ++i) dg[i] = t1n[i] - t1n[i - 1];
+        for (int i = 2; i < k; ++i) dtrn[i] = dg[i] / dg[i - 1];
+    }
+    return true;
+}
+}  // namespace dyn
+
 extern "C" {
 
 int dyn_abi_version(void) { return DYN_ABI_VERSION; }
@@ -718,6 +779,7 @@ dyn_status dyn_state_init(void* p, double delta_t) {
     if ((s = c->mirror_all())) return s;
     c->ctl.delta_t = delta_t > 0 ? delta_t : c->cfg.delta_t_min;
     c->ctl.loop = 0;
+    c->last_rollback_loop = -1000;
     c->ctl.delta = 1;
     c->ctl.delta_old = 0;
     c->ctl.method = c->ctl.delta_t < RMAX[0] / c->specRad ? DYN_RK54 : DYN_SSPRK104;
@@ -960,6 +1022,22 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
         if (s) return s;
         k.delta = r.delta;
         k.loop++;
+        if (rp->sparsify_every > 0 && k.loop % rp->sparsify_every == 0) {
+            // simulation_runner.cpp:148-237: sweeps while the history shrinks, then
+            // (outside a replayed schedule) the step halving
+            size_t prev = c->n;
+            const int sweeps = std::min(10, rp->sparsify_sweeps > 0 ? rp->sparsify_sweeps : 1);
+            for (int sw = 0; sw < sweeps; ++sw) {
+                size_t nn = prev;
+                if ((s = dyn_sparsify(p, dmax, rp->sparsify_variant, &nn))) return s;
+                if (nn >= prev) break;
+                prev = nn;
+            }
+            if (!rp->dt_schedule && k.delta < dmax / 2 && k.loop - c->last_rollback_loop > 1000) {
+                k.delta_t *= 0.5;
+                if (k.method == DYN_RK54) k.method = DYN_SSPRK104;
+            }
+        }
         if (!rp->dt_schedule) {
             const double ratio = c->dtr[c->n - 1];
             if (k.delta < dmax && k.loop > 5 && (k.delta < 1.1 * k.delta_old || k.delta_old < dmax / 1000) &&
@@ -977,6 +1055,7 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
                 const int nr = std::min(10, std::max(0, (int)c->n - 2));
                 if (nr > 0) {
                     if ((s = dyn_rollback(p, nr))) return s;
+                    c->last_rollback_loop = k.loop;
                 }
                 k.delta_t = 0.5 * std::min(std::max(k.delta_t, dmin), RMAX[k.method - 1] / c->specRad);
                 k.method = k.method > 3 ? 2 + (2 * (k.method - 3)) / 2 : DYN_SSPRK104;
@@ -1096,7 +1175,8 @@ dyn_status dyn_adjoint_forward(void* p, const dyn_run_params* rp, dyn_step_resul
     if (!p || !rp) return fail(DYN_ERR_INVALID, "null argument");
     Ctx* c = C(p);
     if (c->d.mixed) return fail(DYN_ERR_UNSUPPORTED, "the adjoint runs on the FP64 form");
-    if (rp->gpu_rollback) return fail(DYN_ERR_INVALID, "the adjoint needs an append-only history: no rollback");
+    if (rp->gpu_rollback || rp->sparsify_every > 0)
+        return fail(DYN_ERR_INVALID, "the adjoint needs an append-only history: no rollback, no sparsify");
     if (c->n == 0) return fail(DYN_ERR_STATE, "no state: call dyn_state_init or dyn_state_upload");
     if (rp->nsteps < 0) return fail(DYN_ERR_INVALID, "nsteps must be non-negative");
     const size_t N = (size_t)rp->nsteps;
@@ -1226,40 +1306,10 @@ dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     cudaFree(fl_d);
     CK(e);
-    std::vector<int> inds;
-    bool erased = false;
-    if (variant == 0) {
-        inds.push_back(0);
-        for (size_t i = 2; i + 1 < n; ++i) {
-            if (fl[i] & 2) erased = true; else inds.push_back((int)i);
-        }
-        inds.push_back((int)n - 1);
-        if (!erased) return DYN_OK;
-    } else if (variant == 1) {
-        int loop = 0;
-        inds.push_back(0);
-        for (size_t i = 2; i + 1 < n; ++i) {
-            if ((fl[i] & 2) && !erased) { erased = true; ++loop; }
-            else { erased = false; ++loop; inds.push_back(loop); }
-        }
-        inds.push_back((int)n - 2);
-        inds.push_back((int)n - 1);
-    } else {
-        for (size_t i = 0; i < n; ++i) if (!(fl[i] & 1) || (fl[i] & 4)) inds.push_back((int)i);
-    }
+    std::vector<int> inds, indsD;
+    std::vector<double> tfac, t1n, dtrn;
+    if (!sparsify_indices(fl.data(), n, variant, c->t1, c->dtr, inds, indsD, tfac, t1n, dtrn)) return DYN_OK;
     const int k = (int)inds.size();
-    std::vector<int> indsD(k, 0);
-    std::vector<double> tfac(k, 1.0);
-    if (variant == 0) {
-        indsD = inds;
-    } else {
-        for (int i = 0; i + 1 < k; ++i) indsD[i + 1] = inds[i] + 1;
-        for (int i = 1; i < k; ++i) {
-            const double num = c->t1[inds[i]] - c->t1[inds[i - 1]];
-            const double den = c->t1[indsD[i]] - c->t1[indsD[i] - 1];
-            tfac[i] = variant == 2 ? (den != 0.0 ? num / den : 1.0) : num / den;
-        }
-    }
     // new buffers sized like the old capacity
     double2 *KRn, *dKRn;
     double *rn, *drn, *dtmp;
@@ -1278,19 +1328,6 @@ dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
     cudaFree(c->d.KR); cudaFree(c->d.dKR); cudaFree(c->d.rvec); cudaFree(c->d.drvec);
     c->d.KR = KRn; c->d.dKR = dKRn; c->d.rvec = rn; c->d.drvec = drn;
     c->drop_graphs();
-    // t1grid by inds; delta_t_ratio per variant (sparsify_utils.cpp:76-96, .cu:99-110)
-    std::vector<double> t1n(k), dtrn;
-    for (int i = 0; i < k; ++i) t1n[i] = c->t1[inds[i]];
-    if (variant == 0) {
-        dtrn.resize(k);
-        for (int i = 0; i < k; ++i) dtrn[i] = c->dtr[inds[i]];
-    } else {
-        dtrn = c->dtr;
-        dtrn.resize(k);
-        std::vector<double> dg(k, 0.0);
-        for (int i = 1; i < k; ++i) dg[i] = t1n[i] - t1n[i - 1];
-        for (int i = 2; i < k; ++i) dtrn[i] = dg[i] / dg[i - 1];
-    }
     c->t1 = t1n;
     c->dtr = dtrn;
     c->n = k;

@@ -53,6 +53,9 @@ struct Plan {
     double dt, delta, delta_old, err_t;
     double T_last, T_prev;  // t1grid[n-1], t1grid[n-2]
     double energy, r, qk0;
+    double dtr_last;        // delta_t_ratio of the newest row (the controller's ratio == 1 test)
+    int spars_loop;         // loop of the last periodic sparsify (-1: none)
+    int last_rb;            // loop of the last rollback (simulation_runner.cpp:53: -1000)
 };
 
 struct Quench {
@@ -61,6 +64,7 @@ struct Quench {
     int cap, rollback;
     long long max_steps;
     double t_stop, dmin, dmax, specRad;
+    long long spars_every;  // periodic sparsify every this many loops (0: never)
 };
 
 struct Work {
@@ -175,7 +179,8 @@ __device__ void begin_step(const Quench& q, Plan& pl, const TabDev& tb) {
 
 // End of a step: the step result and the controller of dyn_run without a
 // schedule (simulation_runner.cpp:252-304), same operation order.
-__device__ void finish_step(const Quench& q, Plan& pl, const StageDev& last, const TabDev& tb) {
+// The step's bookkeeping: error estimate, loop count, the new row's time
+__device__ void finish_step(const Quench& q, Plan& pl, const StageDev& last) {
     const Slots* sl = q.c.slots;
     const double delta = __dadd_rn(sl->res_err, pl.err_t);
     pl.delta_old = pl.delta;
@@ -185,15 +190,25 @@ __device__ void finish_step(const Quench& q, Plan& pl, const StageDev& last, con
     pl.n += 1;
     pl.T_prev = pl.T_last;
     pl.T_last = last.T_next;
+    pl.dtr_last = last.dtr_new;
     pl.energy = sl->res_energy;
     pl.r = sl->res_r;
     pl.qk0 = sl->res_qk0;
+}
 
+// The periodic sparsify falls due at the end of this loop (simulation_runner.cpp:148)
+__device__ __forceinline__ bool sparsify_due(const Quench& q, const Plan& pl) {
+    return q.spars_every > 0 && pl.loop > 0 && pl.loop % q.spars_every == 0 && pl.loop != pl.spars_loop;
+}
+
+// The step-size controller of dyn_run (simulation_runner.cpp:252-304)
+__device__ void adapt_step(const Quench& q, Plan& pl, const TabDev& tb) {
+    const double delta = pl.delta;
     const double dmax = q.dmax, dmin = q.dmin, sr = q.specRad;
     double dt = pl.dt;
     int method = pl.method;
     if (delta < dmax && pl.loop > 5 && (delta < __dmul_rn(1.1, pl.delta_old) || pl.delta_old < __ddiv_rn(dmax, 1000.0)) &&
-        __ddiv_rn(tb.rmax[method - 1], sr) > dt && last.dtr_new == 1.0) {
+        __ddiv_rn(tb.rmax[method - 1], sr) > dt && pl.dtr_last == 1.0) {
         dt = __dmul_rn(dt, 1.01);
     } else if (delta > __dmul_rn(2.0, dmax) && dt > dmin) {
         dt = __dmul_rn(dt, 0.9);
@@ -212,6 +227,7 @@ __device__ void finish_step(const Quench& q, Plan& pl, const StageDev& last, con
             pl.T_prev = q.c.t1grid[target - 2];
             dt = __dsub_rn(pl.T_last, pl.T_prev);
             pl.loop -= nr;
+            pl.last_rb = pl.loop;
             pl.fresh = 1;
         }
         dt = __dmul_rn(0.5, fmin(fmax(dt, dmin), __ddiv_rn(tb.rmax[method - 1], sr)));
@@ -298,13 +314,28 @@ __global__ void __launch_bounds__(EPI_T) k_batch_epi(const Quench* __restrict__ 
         pl.s = s + 1;
         return;
     }
-    finish_step(q, pl, sp, *tb);
+    finish_step(q, pl, sp);
+    if (sparsify_due(q, pl)) {
+        // the host compacts the history, then k_batch_resume adapts and plans
+        pl.status = DYN_QUENCH_SPARSIFY;
+        return;
+    }
+    adapt_step(q, pl, *tb);
     begin_step(q, pl, *tb);
 }
 
 // (Re)start quench b's planning from its plan (after creation, upload or new limits)
 __global__ void k_batch_begin(const Quench* Q, Plan* PL, const TabDev* tb, int b) {
     if (threadIdx.x == 0 && blockIdx.x == 0) begin_step(Q[b], PL[b], *tb);
+}
+
+// Continue quench b after its periodic sparsify: the controller of the loop
+// that ended, then the next step's plan
+__global__ void k_batch_resume(const Quench* Q, Plan* PL, const TabDev* tb, int b) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        adapt_step(Q[b], PL[b], *tb);
+        begin_step(Q[b], PL[b], *tb);
+    }
 }
 
 // ------------------------------------------------------------------ host side
@@ -452,8 +483,111 @@ struct Batch {
 
     int running() const {
         int k = 0;
-        for (const Plan& p : plan_h) k += p.status == DYN_QUENCH_RUNNING;
+        for (const Plan& p : plan_h) k += p.status == DYN_QUENCH_RUNNING || p.status == DYN_QUENCH_SPARSIFY;
         return k;
+    }
+
+    // One sparsify pass over quench b's history (the same flag and compaction
+    // kernels and index logic as dyn_sparsify), in place: rows are compacted
+    // into scratch and copied back, times, FP32 mirrors and the plan's row
+    // count follow.  Call at a step boundary (status other than running).
+    dyn_status sparsify_pass(int b, double thr, int variant, int* n_out) {
+        Quench& q = qh[b];
+        Plan& pl = plan_h[b];
+        const size_t n = (size_t)pl.n, L = q.c.L;
+        *n_out = pl.n;
+        if (n < 3) return DYN_OK;
+        unsigned char* fl_d = nullptr;
+        BCK(cudaMalloc(&fl_d, n));
+        std::vector<unsigned char> fl(n);
+        std::vector<double> t1(n), dtr(n);
+        cudaError_t e = launch_sparsify_flags(q.c, (int)n, variant, thr, fl_d, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fl.data(), fl_d, n, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(t1.data(), q.c.t1grid, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dtr.data(), q.c.dtr, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(fl_d);
+        BCK(e);
+        std::vector<int> inds, indsD;
+        std::vector<double> tfac, t1n, dtrn;
+        if (!sparsify_indices(fl.data(), n, variant, t1, dtr, inds, indsD, tfac, t1n, dtrn)) return DYN_OK;
+        const size_t k = inds.size();
+        double2 *KRn = nullptr, *dKRn = nullptr;
+        double *rn = nullptr, *drn = nullptr, *tf = nullptr;
+        int* id = nullptr;
+        auto release = [&]() {
+            cudaFree(KRn); cudaFree(dKRn); cudaFree(rn); cudaFree(drn); cudaFree(tf); cudaFree(id);
+        };
+        if ((e = cudaMalloc(&KRn, k * L * sizeof(double2))) != cudaSuccess ||
+            (e = cudaMalloc(&dKRn, k * L * sizeof(double2))) != cudaSuccess ||
+            (e = cudaMalloc(&rn, k * sizeof(double))) != cudaSuccess ||
+            (e = cudaMalloc(&drn, k * sizeof(double))) != cudaSuccess ||
+            (e = cudaMalloc(&tf, k * sizeof(double))) != cudaSuccess ||
+            (e = cudaMalloc(&id, 2 * k * sizeof(int))) != cudaSuccess) {
+            release();
+            return bfail(DYN_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        std::vector<double> inv(k);
+        for (size_t r = 0; r < k; ++r) inv[r] = dtrn[r] != 0.0 ? 1.0 / dtrn[r] : 0.0;
+        const bool ok =
+            cudaMemcpyAsync(id, inds.data(), k * sizeof(int), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(id + k, indsD.data(), k * sizeof(int), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(tf, tfac.data(), k * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            launch_compact(q.c, id, id + k, variant == 0 ? nullptr : tf, (int)k, KRn, dKRn, rn, drn, st) == cudaSuccess &&
+            cudaMemcpyAsync(q.c.KR, KRn, k * L * sizeof(double2), cudaMemcpyDeviceToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(q.c.dKR, dKRn, k * L * sizeof(double2), cudaMemcpyDeviceToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(q.c.rvec, rn, k * sizeof(double), cudaMemcpyDeviceToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(q.c.drvec, drn, k * sizeof(double), cudaMemcpyDeviceToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(q.c.t1grid, t1n.data(), k * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(q.c.dtr, dtrn.data(), k * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(q.c.inv_dtr, inv.data(), k * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            launch_mirror_rows(q.c.KR, q.c.KRf, k * L, st) == cudaSuccess &&
+            launch_mirror_rows(q.c.dKR, q.c.dKRf, k * L, st) == cudaSuccess &&
+            launch_time_f32(q.c.t1grid, q.c.dtr, (int)k, q.c.inv_len_f, q.c.inv_dtr_f, st) == cudaSuccess;
+        e = cudaStreamSynchronize(st);  // the host vectors above are sources of the copies
+        release();
+        if (!ok || e != cudaSuccess) return bfail(DYN_ERR_CUDA, "batch sparsify: " + std::string(cudaGetErrorString(cudaGetLastError())));
+        pl.n = (int)k;
+        pl.T_last = t1n[k - 1];
+        pl.T_prev = k >= 2 ? t1n[k - 2] : 0.0;
+        pl.dtr_last = dtrn[k - 1];
+        pl.fresh = 1;
+        *n_out = (int)k;
+        return DYN_OK;
+    }
+
+    // Quenches paused for their periodic sparsify (simulation_runner.cpp:148-237):
+    // passes while the history shrinks, then the step halving when delta <
+    // delta_max/2 and the last rollback is more than 1000 loops back, then the
+    // controller of the loop and the next step's plan on the device.
+    dyn_status service_sparsify() {
+        bool any = false;
+        for (size_t b = 0; b < qh.size(); ++b) {
+            if (plan_h[b].status != DYN_QUENCH_SPARSIFY) continue;
+            any = true;
+            Plan& pl = plan_h[b];
+            const double dmax = qh[b].dmax;
+            const int sweeps = std::min(10, cfg.sparsify_sweeps > 0 ? cfg.sparsify_sweeps : 1);
+            int prev = pl.n;
+            for (int sw = 0; sw < sweeps; ++sw) {
+                int nn = prev;
+                dyn_status s = sparsify_pass((int)b, dmax, cfg.sparsify_variant, &nn);
+                if (s) return s;
+                if (nn >= prev) break;
+                prev = nn;
+            }
+            if (pl.delta < dmax / 2 && pl.loop - pl.last_rb > 1000) {
+                pl.dt *= 0.5;
+                if (pl.method == DYN_RK54) pl.method = DYN_SSPRK104;
+            }
+            pl.spars_loop = pl.loop;
+            pl.status = DYN_QUENCH_RUNNING;
+            BCK(cudaMemcpyAsync(pd + b, &pl, sizeof(Plan), cudaMemcpyHostToDevice, st));
+            k_batch_resume<<<1, 32, 0, st>>>(qd, pd, tabd, (int)b);
+            BCK(cudaGetLastError());
+            BCK(cudaStreamSynchronize(st));  // &pl is host memory the copy reads
+        }
+        return any ? read_plans() : DYN_OK;
     }
 
     dyn_status enqueue_ticks(int n) {
@@ -509,6 +643,9 @@ struct Batch {
         p.fresh = 1;
         p.T_last = 0.0;
         p.T_prev = 0.0;
+        p.dtr_last = 0.0;
+        p.spars_loop = -1;
+        p.last_rb = -1000;
         BCK(cudaMemcpyAsync(pd + b, &p, sizeof(Plan), cudaMemcpyHostToDevice, st));
         BCK(cudaStreamSynchronize(st));  // the host vectors above are stack memory
         return begin(b);
@@ -530,6 +667,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
     *out = nullptr;
     if (ngrids < 1 || nquench < 1 || nquench > 65535) return bfail(DYN_ERR_INVALID, "need 1..65535 quenches and at least one grid");
     if (cfg->search != DYN_SEARCH_BINARY && cfg->search != DYN_SEARCH_LOWER_BOUND) return bfail(DYN_ERR_INVALID, "unknown search");
+    if (cfg->sparsify_variant < 0 || cfg->sparsify_variant > 2) return bfail(DYN_ERR_INVALID, "unknown sparsify variant");
     for (int g = 0; g < ngrids; ++g) {
         const size_t L = grids[g].len, m = grids[g].depth;
         if (L < 4 || L > 4096 || m < 2 || m > L) return bfail(DYN_ERR_INVALID, "len must be in [4, 4096] and 2 <= depth <= len");
@@ -672,6 +810,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         cudaMemset(q.stg, 0, 2 * SMAX * sizeof(StageDev));
         q.cap = (int)cap;
         q.rollback = cfg->gpu_rollback ? 1 : 0;
+        q.spars_every = cfg->sparsify_every > 0 ? cfg->sparsify_every : 0;
         q.max_steps = sq.max_steps;
         q.t_stop = sq.t_stop;
         q.dmin = sq.delta_t_min;
@@ -771,6 +910,9 @@ dyn_status dyn_batch_upload(void* p, int qi, const dyn_state* stt, const dyn_con
     pl.method = ctl->method;
     pl.fresh = 1;
     pl.sidx = 0;
+    pl.dtr_last = stt->delta_t_ratio[n - 1];
+    pl.spars_loop = -1;
+    pl.last_rb = -1000;
     BCK(cudaMemcpyAsync(bt->pd + qi, &pl, sizeof(Plan), cudaMemcpyHostToDevice, st));
     BCK(cudaStreamSynchronize(st));
     dyn_status s = bt->begin(qi);
@@ -861,6 +1003,7 @@ dyn_status dyn_batch_run(void* p, long long max_ticks, long long* ticks_out) {
             done = max_ticks;
         }
         if ((s = bt->read_plans())) return s;
+        if ((s = bt->service_sparsify())) return s;
     }
     if (ticks_out) *ticks_out = done;
     return DYN_OK;
@@ -878,7 +1021,8 @@ dyn_status dyn_batch_enqueue(void* p, long long ticks) {
 
 dyn_status dyn_batch_sync(void* p) {
     if (!p) return bfail(DYN_ERR_INVALID, "null argument");
-    return BT(p)->read_plans();
+    dyn_status s = BT(p)->read_plans();
+    return s ? s : BT(p)->service_sparsify();
 }
 
 dyn_status dyn_batch_last_row(void* p, int qi, double* qK, double* qR) {

@@ -61,4 +61,11 @@ void set_last_error(const std::string& msg);
 // Validates a table set and returns the stencil starts as int32 (dyn_api.cu)
 bool check_tables(size_t L, size_t m, const dyn_tables* tb, std::vector<int> i32[3], std::string& why);
 
+// Keep list, derivative rows with their time factors, and the new t1grid /
+// delta_t_ratio of one sparsify pass from its node flags (dyn_api.cu); false
+// when variant 0 erases nothing
+bool sparsify_indices(const unsigned char* fl, size_t n, int variant, const std::vector<double>& t1,
+                      const std::vector<double>& dtr, std::vector<int>& inds, std::vector<int>& indsD,
+                      std::vector<double>& tfac, std::vector<double>& t1n, std::vector<double>& dtrn);
+
 }  // namespace dyn

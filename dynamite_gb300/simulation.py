@@ -212,7 +212,11 @@ class Simulation:
     def SERK2(self, q: int, delta_t: float) -> StepResult:
         return self.update(serk2_method(q), delta_t)
 
-    def run(self, nsteps: int, schedule=None, tmax: float = 0.0, gpu_rollback: bool = False) -> dict:
+    def run(self, nsteps: int, schedule=None, tmax: float = 0.0, gpu_rollback: bool = False,
+            sparsify_every: int = 0, sparsify_sweeps: int = 1, sparsify_variant: str = "gpu") -> dict:
+        """The driver loop (simulation_runner.cpp:125-304): `nsteps` controller iterations
+        (or until t >= tmax); with `sparsify_every` > 0 the periodic sparsify of the
+        reference (every that many loops; the reference uses 100000)."""
         out = {k: np.zeros(nsteps) for k in ("dt", "delta", "t", "energy", "qk0", "r")}
         meth = np.zeros(nsteps, dtype=np.int32)
         sd = sm = None
@@ -222,7 +226,8 @@ class Simulation:
         rp = _lib.RunParams(nsteps, tmax, _lib.ptr(sd), None if sm is None else sm.ctypes.data_as(_lib.ip),
                             int(gpu_rollback), _lib.ptr(out["dt"]), meth.ctypes.data_as(_lib.ip),
                             _lib.ptr(out["delta"]), _lib.ptr(out["t"]), _lib.ptr(out["energy"]),
-                            _lib.ptr(out["qk0"]), _lib.ptr(out["r"]))
+                            _lib.ptr(out["qk0"]), _lib.ptr(out["r"]), sparsify_every, sparsify_sweeps,
+                            SPARSIFY[sparsify_variant])
         last = _lib.StepResult()
         _lib.check(_lib.lib().dyn_run(self._h, C.byref(rp), C.byref(last)), "dyn_run")
         out["method"] = meth

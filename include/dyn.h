@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DYN_ABI_VERSION 1
+#define DYN_ABI_VERSION 2
 
 typedef enum {
     DYN_OK = 0,
@@ -147,6 +147,15 @@ typedef struct {
     double* out_energy;
     double* out_qk0;
     double* out_r;
+    /* periodic sparsify of the driver loop (simulation_runner.cpp:148-237): after
+     * every loop that is a multiple of sparsify_every (0: never; the reference
+     * uses 100000), up to sparsify_sweeps passes of dyn_sparsify(delta_max,
+     * sparsify_variant) while the history shrinks (<= 0: one pass, at most 10),
+     * then, if delta < delta_max/2 and the last rollback is more than 1000
+     * loops back, delta_t halves and RK54 gives way to SSPRK(10,4) */
+    long long sparsify_every;
+    int sparsify_sweeps;
+    int sparsify_variant;
 } dyn_run_params;
 
 /* ---------------------------------------------------------------- basics */
@@ -287,6 +296,13 @@ typedef struct {
     int threads;             /* gather CTA threads: 128 or 256 (0: 128) */
     int targets;             /* targets per thread: 1 or 2 (0: 1) */
     int ctas_per_sm;         /* persistent gather CTAs per SM (0: occupancy limit) */
+    /* periodic sparsify of every quench, as dyn_run_params (threshold: the
+     * quench's delta_max); a quench pauses at the end of such a loop with
+     * status DYN_QUENCH_SPARSIFY until the host has compacted its history
+     * (dyn_batch_run, dyn_batch_sync) */
+    long long sparsify_every;
+    int sparsify_sweeps;
+    int sparsify_variant;
 } dyn_batch_config;
 
 /* Quench status */
@@ -294,7 +310,8 @@ enum {
     DYN_QUENCH_RUNNING = 0,
     DYN_QUENCH_DONE = 1,      /* reached t_stop */
     DYN_QUENCH_MAXSTEPS = 2,  /* took max_steps steps */
-    DYN_QUENCH_FULL = 3       /* history capacity reached */
+    DYN_QUENCH_FULL = 3,      /* history capacity reached */
+    DYN_QUENCH_SPARSIFY = 4   /* waiting for its periodic sparsify (transient) */
 };
 
 typedef struct {

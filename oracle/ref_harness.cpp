@@ -258,10 +258,15 @@ void dynref_sparsify(double threshold) { sparsifyNscale(threshold); }
 // replayed instead of adapted (frozen schedule).  Per step it records the
 // step size used, the method, the error estimate and the energy
 // (simulation_runner.cpp:334-336) at the loop's own t (:128).
+// With sparsify_every > 0 the periodic block of :148-237 (CPU branch: one
+// sparsifyNscale pass at delta_max, interpolate(), then the halving with
+// rk->init = 2 when delta < delta_max/2; no rollback on the CPU, so the last
+// rollback loop stays at its initial -1000, :53).
 int dynref_run(int nsteps, const double* schedule_dt, const int* schedule_method,
                double* out_dt, int* out_method, double* out_delta, double* out_t,
-               double* out_energy) {
+               double* out_energy, long long sparsify_every) {
     const size_t L = config.len;
+    const int last_rollback_loop = -1000;
     for (int k = 0; k < nsteps; ++k) {
         if (schedule_dt) {
             config.delta_t = schedule_dt[k];
@@ -273,6 +278,14 @@ int dynref_run(int nsteps, const double* schedule_dt, const int* schedule_method
         config.delta_old = config.delta;
         config.delta = update();
         config.loop++;
+        if (sparsify_every > 0 && config.loop % sparsify_every == 0) {
+            sparsifyNscale(config.delta_max);
+            interpolate();
+            if (!schedule_dt && config.delta < config.delta_max / 2 && config.loop - last_rollback_loop > 1000) {
+                config.delta_t *= 0.5;
+                rk->init = 2;
+            }
+        }
         if (!schedule_dt) {
             if (config.delta < config.delta_max && config.loop > 5 &&
                 (config.delta < 1.1 * config.delta_old || config.delta_old < config.delta_max / 1000) &&

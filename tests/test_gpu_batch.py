@@ -137,3 +137,34 @@ def test_batch_autotuned_tiles(product_built):
             assert rel_err(sa.QK, sb.QK) < MIXED_TRAJ_TOL
             assert rel_err(sa.rvec, sb.rvec) < MIXED_TRAJ_TOL
         assert abs(b.info(q)["energy"] - tr["energy"][-1]) <= MIXED_TRAJ_TOL * abs(tr["energy"][-1])
+
+
+def test_batch_periodic_sparsify_equals_single(product_built):
+    """The reference driver's periodic sparsify (every 20 loops here) inside a batch: each
+    quench pauses at the end of the loop, the host compacts its history, the controller
+    and planner resume on the device; the result equals dyn_run with the same cadence."""
+    grids, m32, m64 = _grids()
+    kw = dict(vars(m32))
+    kw["delta_max"] = 1e-7
+    m = D.Model(**kw)
+    kw2 = dict(vars(m64))
+    kw2["delta_max"] = 1e-7
+    m2 = D.Model(**kw2)
+    specs = [(0, m, 70), (1, m2, 45)]
+    for variant in ("gpu", "cpu"):
+        b = D.Batch(grids, [_quench(gi, mm, max_steps=n) for gi, mm, n in specs], ticks_per_launch=16,
+                    sparsify_every=20, sparsify_variant=variant)
+        b.run(100_000)
+        for q, (gi, mm, n) in enumerate(specs):
+            inf = b.info(q)
+            assert inf["status"] == "max_steps" and inf["steps"] == n
+            s = D.Simulation(grids[gi], mm, precision="mixed")
+            s.init()
+            tr = s.run(n, sparsify_every=20, sparsify_variant=variant)
+            st = s.download()
+            assert st.t1grid.size < n + 1  # rows were dropped
+            _assert_same_state(b.download(q), st)
+            c = s.controller
+            assert (inf["delta_t"], inf["method"], inf["loop"]) == (c["delta_t"], c["method"], c["loop"])
+            assert inf["energy"] == tr["energy"][-1]
+        b.close()

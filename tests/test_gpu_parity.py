@@ -260,3 +260,57 @@ def test_polynomial_history_is_reproduced(product_built):
     assert np.max(np.abs(s.interp(1) - Q(grid.phi1))) < 1e-12
     assert np.max(np.abs(s.interp(2) - P(grid.phi2))) < 1e-12
     assert np.max(np.abs(s.interp(3) - Q(grid.phi2))) < 1e-12
+
+
+def _spars_model(g, M):
+    """The golden model with a delta_max at which sparsify drops rows of a short run."""
+    kw = dict(vars(model_from(g, M)))
+    kw["delta_max"] = 1e-7
+    return M(**kw)
+
+
+@pytest.mark.parametrize("variant", [0, 2])
+def test_periodic_sparsify_fixed_schedule(product_built, variant):
+    """dyn_run's periodic block (simulation_runner.cpp:148-237) against the oracle: the
+    oracle runs its own controller with a sparsify every 20 loops, the GPU replays
+    that schedule with the same cadence; time grids and keep decisions bit-exact."""
+    g = load_golden(32)
+    p = O.Port(grid_from(g, O.Grid), _spars_model(g, O.Model), search_mode=1, threads=4)
+    p.init_state()
+    tr = p.run(70, sparsify_every=20, sparsify_variant=variant)
+    s = D.Simulation(grid_from(g, D.Grid), _spars_model(g, D.Model))
+    s.init()
+    tg = s.run(70, schedule=(tr["dt"], tr["method"]), sparsify_every=20,
+               sparsify_variant=["cpu", "cuda_host", "gpu"][variant])
+    a, b = s.download(), p.get_state()
+    assert a.t1grid.size < 71
+    np.testing.assert_array_equal(a.t1grid, b.t1grid)
+    np.testing.assert_array_equal(a.dtr, b.dtr)
+    for k in ("QK", "QR", "dQK", "dQR", "rvec", "drvec"):
+        assert rel_err(getattr(a, k), getattr(b, k)) < TRAJ_TOL, k
+    assert rel_err(tg["energy"], tr["energy"]) < TRAJ_TOL
+
+
+def test_periodic_sparsify_free_controller(product_built):
+    """A free run with the cadence (sparsify, then the step-halving rule, then the
+    usual adaptation) makes the oracle's decisions, except where an error estimate
+    sits within rounding of a threshold."""
+    g = load_golden(32)
+    p = O.Port(grid_from(g, O.Grid), _spars_model(g, O.Model), search_mode=1, threads=4)
+    p.init_state()
+    tr = p.run(70, sparsify_every=20, sparsify_variant=2)
+    s = D.Simulation(grid_from(g, D.Grid), _spars_model(g, D.Model))
+    s.init()
+    tg = s.run(70, sparsify_every=20, sparsify_variant="gpu")
+    same = (tg["dt"] == tr["dt"]) & (tg["method"] == tr["method"])
+    if not same.all():
+        k = int(np.argmin(same))
+        d, dmax = tr["delta"][k - 1], 1e-7
+        near = min(abs(d - dmax), abs(d - 2 * dmax), abs(d - dmax / 2), abs(d - 1.1 * tr["delta"][k - 2])) / dmax
+        assert near < 1e-3, f"schedules diverge at step {k} away from a threshold"
+    else:
+        a, b = s.download(), p.get_state()
+        np.testing.assert_array_equal(a.t1grid, b.t1grid)
+        assert rel_err(a.QK, b.QK) < TRAJ_TOL
+        c = s.controller
+        assert (c["delta_t"], c["method"]) == p.controller()

@@ -152,3 +152,23 @@ def test_serk_coefficients_consistent(oracle_built):
         b = O.Port.serk_coeffs(q)
         assert b.size == 2 * q + 1
         assert abs(b.sum() - 1.0) < 1e-12
+
+
+@pytest.mark.skipif(not O.Reference.available(), reason="reference sources not built here")
+def test_port_equals_reference_with_periodic_sparsify(oracle_built):
+    """The driver loop's periodic block (simulation_runner.cpp:148-237, CPU branch):
+    sparsify every 20 loops at delta_max, interpolate, halve delta_t when delta < delta_max/2."""
+    g = O.Reference.grid(48, Tmax=20.0)
+    m = O.Model(p=3, p2=4, lam=0.3, Gamma=0.7, delta_max=1e-7)
+    port = O.Port(g, m, search_mode=0, threads=1)
+    ref = O.Reference(g, m, threads=1)
+    ref.init_state()
+    port.init_state()
+    r1, r2 = ref.run(70, sparsify_every=20), port.run(70, sparsify_every=20, sparsify_variant=0)
+    for k in r1:
+        np.testing.assert_array_equal(r1[k], r2[k], err_msg=k)
+    s1, s2 = ref.get_state(), port.get_state()
+    assert s1.t1grid.size < 71  # rows were dropped
+    for k in STATE_FIELDS:
+        np.testing.assert_array_equal(getattr(s1, k), getattr(s2, k), err_msg=k)
+    assert (O.Reference.lib().dynref_get_delta_t(), O.Reference.lib().dynref_get_method()) == port.controller()
