@@ -215,6 +215,31 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def replica_barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def replica_reduce(x: float, world: int, op: str) -> float:
+    """x summed ("sum") or maximised ("max") over the replicas (one per GPU, no data exchange
+    on the path: only these timing scalars cross ranks)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.SUM if op == "sum" else dist.ReduceOp.MAX)
+    return float(tt[0])
+
+
+def job_rate(steps_local: int, seconds_local: float, world: int):
+    """Whole-job throughput of N replicas: RK steps of all ranks / the slowest rank's time."""
+    steps = replica_reduce(float(steps_local), world, "sum")
+    t = replica_reduce(seconds_local, world, "max")
+    return int(steps), t, steps / t
+
+
 def _stages(m: int) -> int:
     return 7 if m == 1 else (10 if m == 2 else 4 * (m - 2))
 
@@ -400,17 +425,10 @@ def run_ours(args):
     cap = args.setup + args.warmup + 2 * args.steps + 64
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replica_barrier(world)
 
     def max_over_ranks(x):
-        if world > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([x], dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            return float(tt[0])
-        return x
+        return replica_reduce(x, world, "max")
 
     # ---- plain FP64 and single-quench mixed forms (the comparison points)
     fp64, cpu_state, start = _fp64_single(D, torch, args, grid, dev, stream, flush, cap)
@@ -439,9 +457,7 @@ def run_ours(args):
     barrier()
     bt.sync()
     rk_steps = bt.total_steps() - steps0
-    t_batch = max_over_ranks(e0.elapsed_time(e1) / 1e3)
-    rk_steps_all = rk_steps * world
-    value = rk_steps_all / t_batch
+    rk_steps_all, t_batch, value = job_rate(rk_steps, e0.elapsed_time(e1) / 1e3, world)
 
     # ---- end to end through the C ABI: dyn_batch_run with its status reads, plus every
     #      quench's newest row C(t, theta t), R(t, theta t) read back after each launch
@@ -454,8 +470,7 @@ def run_ours(args):
         bt.run(32)
         for q in range(B):
             bt.last_row(q, *rows[q])
-    t_e2e = max_over_ranks(time.perf_counter() - t0)
-    e2e_steps = (bt.total_steps() - s0) * world
+    e2e_steps, t_e2e, _ = job_rate(bt.total_steps() - s0, time.perf_counter() - t0, world)
     d2h_tick = (B * 112 + B * 2 * args.L * 8) / 32.0
 
     if rank != 0:
