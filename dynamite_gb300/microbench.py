@@ -13,6 +13,7 @@ the staggered derivatives (t_k - t_{k-1}) d/dt C(t, theta_j t) at t_{k-1}
 
     python -m dynamite_gb300.microbench --form adjoint --L 512 --steps 20
     python -m dynamite_gb300.microbench --form mixed_error --L 1024 --steps 5000
+    python -m dynamite_gb300.microbench --form long --L 512 --steps 400000 --tmax 1e6
 
 `fp64` / `mixed` time the single-quench gather+convolution kernel and the
 epilogue (one right-hand side at t = t_{n-1}); `batch` times the batched
@@ -23,7 +24,11 @@ d(T, lam), and reports both wall times; `mixed_error` runs the FP64 form of
 that quench for `steps` steps and replays its step schedule in the mixed
 form, then reports the relative error of the mixed run per observable:
 energy over the run, r(t), C and R over the whole history, the equal-time
-C(t, t), and at the final time t_f C(t_f/2, t_f) and R(t_f, t_f/2).
+C(t, t), and at the final time t_f C(t_f/2, t_f) and R(t_f, t_f/2); `long`
+runs the FP64 form from t=0 to `tmax` (at most `steps` steps) with the
+reference driver's periodic sparsify every 100000 loops, then the mixed
+form on that step schedule, and reports steps, wall times, history sizes and
+the final-time observables of both.
 Prints one JSON line.
 """
 from __future__ import annotations
@@ -91,9 +96,41 @@ def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5, tmax:
             "C_tf_half_tf": abs(c_b - c_a) / abs(c_a), "R_tf_tf_half": abs(r_b - r_a) / abs(r_a)}
 
 
+def long_run(grid: Grid, nmax: int, tmax: float, T: float = 0.6, lam: float = 0.5, every: int = 100000) -> dict:
+    """FP64 run to tmax with the periodic sparsify, then the mixed form on its schedule."""
+    import time
+    from .grid import lagrange_weights
+    from .simulation import Model, Simulation
+    L = grid.L
+    m = Model(p=3, p2=4, lam=lam, Gamma=T)
+    w = lagrange_weights(grid.theta, 0.5)
+    out = {"form": "long", "L": L, "tmax": tmax, "T": T, "lam": lam, "sparsify_every": every}
+    sched = None
+    for prec in ("fp64", "mixed"):
+        s = Simulation(grid, m, precision=prec, history_capacity=min(nmax, every) + 64)
+        s.init()
+        t0 = time.perf_counter()
+        if sched is None:
+            tr = s.run(nmax, tmax=tmax, sparsify_every=every)
+            done = int(np.count_nonzero(tr["dt"]))
+            sched = (tr["dt"][:done], tr["method"][:done])
+        else:
+            tr = s.run(sched[0].size, schedule=sched, sparsify_every=every)
+        sec = time.perf_counter() - t0
+        st = s.download()
+        last_K, last_R = st.QK[-L:], st.QR[-L:]
+        out[prec] = {"steps": int(sched[0].size), "seconds": sec, "steps_per_s": sched[0].size / sec,
+                     "t_final": float(st.t1grid[-1]), "history_rows": int(st.t1grid.size), "energy": s.energy(),
+                     "r": float(st.rvec[-1]), "C_tf_half_tf": float(w @ last_K), "R_tf_tf_half": float(w @ last_R)}
+        s.close()
+    a, b = out["fp64"], out["mixed"]
+    out["mixed_rel_err"] = {k: abs(b[k] - a[k]) / abs(a[k]) for k in ("energy", "r", "C_tf_half_tf", "R_tf_tf_half")}
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error"], default="batch")
+    ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error", "long"], default="batch")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--tmax", type=float, default=0.0, help="mixed_error: run the FP64 form to t >= tmax")
     ap.add_argument("--L", type=int, default=512)
@@ -117,6 +154,9 @@ def main(argv=None):
         s.close()
         print(json.dumps({"form": "adjoint", "L": a.L, "steps": a.steps, "t_final": float(fw["t"][-1]),
                           "dE_dT": float(g[0]), "dE_dlam": float(g[1]), **stats}))
+        return
+    if a.form == "long":
+        print(json.dumps(long_run(grid, a.steps, a.tmax, a.T)))
         return
     if a.form == "mixed_error":
         print(json.dumps(mixed_error(grid, a.steps, a.T, tmax=a.tmax)))
