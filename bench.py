@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--config4-setup", type=int, default=1000,
                     help="untimed steps of every quench of the mixed-L batch before its timed ticks (0: skip it)")
     ap.add_argument("--adjoint-steps", type=int, default=5000, help="FP64 steps of the adjoint measurement (0: skip)")
+    ap.add_argument("--no-df", dest="df", action="store_false", help="skip the batched (hi, lo) form")
     return ap.parse_args()
 
 
@@ -312,6 +313,33 @@ def _batch_alg_bytes(L: int, m: int, rows) -> float:
     return 3 * L * L * (4 * m + 4) + 8 * L * L + sum(16 * L * n + 64 * L for n in rows)
 
 
+def _batch_df(D, torch, args, grid, dev, stream):
+    """The headline workload in the (hi, lo) form (precision mixed_df): same quenches, same
+    setup, `steps` ticks timed."""
+    B = args.quenches
+    cap = args.setup + args.warmup + args.steps + 64
+    bt = D.Batch([grid], _batch_quenches(D, B, args.setup, cap), ticks_per_launch=32, device=dev,
+                 stream=stream.cuda_stream, precision="mixed_df")
+    bt.run(10 ** 9)
+    for q in range(B):
+        bt.set_limits(q, max_steps=10 ** 12)
+    bt.run(args.warmup)
+    steps0 = bt.total_steps()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    bt.enqueue(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    bt.sync()
+    t = e0.elapsed_time(e1) / 1e3
+    steps = bt.total_steps() - steps0
+    out = {"value": steps / t, "unit": UNIT, "ms_per_tick": 1e3 * t / args.steps, "rk_steps_timed": steps,
+           "ms_gather": bt.profile(reps=5)}
+    bt.close()
+    return out
+
+
 def _config4(D, torch, args, dev, stream):
     """The mixed-L batch: 64 quenches, temperatures uniform on [0.4, 1.0], lambda cycling
     0.3/0.5/0.7, grid length from {256, 512, 1024} and stopping time log-uniform on [1e4, 1e7]
@@ -475,6 +503,7 @@ def run_ours(args):
 
     if rank != 0:
         return
+    batch_df = _batch_df(D, torch, args, grid, dev, stream) if args.df else None
     config4 = _config4(D, torch, args, dev, stream) if args.config4_setup > 0 else None
     adjoint = _adjoint(D, torch, args, dev) if args.adjoint_steps > 0 else None
     # ---- roofline of the dominant kernel: the batched gather, timed live on its stream
@@ -512,6 +541,8 @@ def run_ours(args):
                                      "flop_per_launch": fp64_flop, "kernel": "k_main (FP64 fused gather)",
                                      "peak_source": "measured (dyn_probe_fp64, same run)"}),
         "mixed_single": mixed,
+        "batched_mixed_df": None if batch_df is None else dict(batch_df, speedup_vs_fp64=batch_df["value"] / fp64["value"],
+                                                                 note="the (hi, lo) form: ~100x smaller long-run error"),
         "config4_mixed_L": config4,
         "adjoint": adjoint,
         "e2e": {"value": e2e_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,

@@ -52,7 +52,7 @@ class Batch:
     def __init__(self, grids: list[Grid], quenches: list[Quench], search: str = "binary", gpu_rollback: bool = False,
                  ticks_per_launch: int = 32, threads: int = 128, targets: int = 1, ctas_per_sm: int = 0,
                  device: int = 0, stream: int | None = None, sparsify_every: int = 0, sparsify_sweeps: int = 1,
-                 sparsify_variant: str = "gpu"):
+                 sparsify_variant: str = "gpu", precision: str = "mixed"):
         self.grids = grids
         self.quenches = list(quenches)
         self._h = C.c_void_p()
@@ -70,7 +70,8 @@ class Batch:
             qs[k] = _lib.BatchQuench(q.grid, q.p, q.p2, q.lam, q.T0, q.Gamma, q.delta_t_min, q.delta_max, q.delta_t,
                                      q.t_stop, q.max_steps, q.capacity)
         cfg = _lib.BatchConfig(device, stream, SEARCH[search], int(gpu_rollback), ticks_per_launch, threads, targets,
-                               ctas_per_sm, sparsify_every, sparsify_sweeps, SPARSIFY[sparsify_variant])
+                               ctas_per_sm, sparsify_every, sparsify_sweeps, SPARSIFY[sparsify_variant],
+                               {"mixed": 1, "mixed_df": 2}[precision])
         _lib.check(_lib.lib().dyn_batch_create(C.byref(cfg), gs, len(grids), qs, len(quenches), C.byref(self._h)),
                    "dyn_batch_create")
         del keep  # the tables were copied to the device

@@ -113,7 +113,8 @@ struct Ctx {
                         d.rvec, d.drvec, d.posB1x, d.posB1x_next, d.posB1x_saved, d.posB2x, d.posB2x_saved, d.h, d.gS,
                         d.geS, d.gfS, d.part, d.rowval, d.epart, d.slots, d.stages, d.rhs_out, d.ip,
                         d.rint, scratch_dev, (void*)d.wA1f, (void*)d.wA2f, (void*)d.wB2f, d.KRf, d.dKRf,
-                        (void*)d.integ_f, d.inv_len_f, d.inv_dtr_f};
+                        (void*)d.integ_f, d.inv_len_f, d.inv_dtr_f, d.KRl, (void*)d.wA1l, (void*)d.wA2l,
+                        (void*)d.wB2l};
         for (void* b : bufs) if (b) cudaFree(b);
         std::memset(&d, 0, sizeof d);
         scratch_dev = nullptr;
@@ -144,15 +145,19 @@ struct Ctx {
         // +16 elements: the 16-byte segment loads of the mixed kernel may touch
         // one element past the end of the last row
         if (d.mixed && ((s = dalloc(&KRf, ncap * L + 16)) || (s = dalloc(&dKRf, ncap * L + 16)))) return s;
+        float2* KRl = nullptr;
+        if (d.mixed == 2 && (s = dalloc(&KRl, ncap * L + 16))) return s;
         // rows not written yet meet the zero taps of the gather segments: keep them finite
         if (d.mixed) {
             CK(cudaMemsetAsync(KRf, 0, (ncap * L + 16) * sizeof(float2), st));
             CK(cudaMemsetAsync(dKRf, 0, (ncap * L + 16) * sizeof(float2), st));
         }
+        if (KRl) CK(cudaMemsetAsync(KRl, 0, (ncap * L + 16) * sizeof(float2), st));
         if (n && d.mixed) {
             CK(cudaMemcpyAsync(KRf, d.KRf, n * L * sizeof(float2), cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(dKRf, d.dKRf, n * L * sizeof(float2), cudaMemcpyDeviceToDevice, st));
         }
+        if (n && KRl) CK(cudaMemcpyAsync(KRl, d.KRl, n * L * sizeof(float2), cudaMemcpyDeviceToDevice, st));
         if (n) {
             CK(cudaMemcpyAsync(KR, d.KR, n * L * sizeof(double2), cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(dKR, d.dKR, n * L * sizeof(double2), cudaMemcpyDeviceToDevice, st));
@@ -172,8 +177,10 @@ struct Ctx {
             if (d.dKRf) cudaFree(d.dKRf);
             if (d.inv_len_f) cudaFree(d.inv_len_f);
             if (d.inv_dtr_f) cudaFree(d.inv_dtr_f);
+            if (d.KRl) cudaFree(d.KRl);
             d.KRf = KRf;
             d.dKRf = dKRf;
+            d.KRl = KRl;
             d.inv_len_f = ilen;
             d.inv_dtr_f = idtf;
             if (n) CK(launch_time_f32(d.t1grid, d.dtr, (int)n, d.inv_len_f, d.inv_dtr_f, st));
@@ -199,6 +206,7 @@ struct Ctx {
         if (!d.mixed || n == 0) return DYN_OK;
         CK(launch_mirror_rows(d.KR, d.KRf, n * L, st));
         CK(launch_mirror_rows(d.dKR, d.dKRf, n * L, st));
+        if (d.KRl) CK(launch_mirror_lo(d.KR, d.KRl, n * L, st));
         return DYN_OK;
     }
 
@@ -651,7 +659,8 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     *out = nullptr;
     const size_t L = cfg->len, m = cfg->depth;
     if (L < 4 || L > 4096 || m < 2 || m > L) return fail(DYN_ERR_INVALID, "len must be in [4, 4096] and 2 <= depth <= len");
-    if (cfg->precision != DYN_FP64 && cfg->precision != DYN_MIXED) return fail(DYN_ERR_INVALID, "unknown precision");
+    if (cfg->precision != DYN_FP64 && cfg->precision != DYN_MIXED && cfg->precision != DYN_MIXED_DF)
+        return fail(DYN_ERR_INVALID, "unknown precision");
     const size_t L2 = L * L;
     std::vector<int> i32[3];
     {
@@ -677,7 +686,7 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     d.L = (int)L;
     d.m = (int)m;
     d.search = cfg->search;
-    d.mixed = cfg->precision == DYN_MIXED;
+    d.mixed = cfg->precision == DYN_MIXED ? 1 : cfg->precision == DYN_MIXED_DF ? 2 : 0;
     // tile shape: threads per CTA x targets per thread.  FP64: few wide CTAs
     // amortize the FP64 reduction; mixed: one target per thread keeps more
     // warps in flight for the latency-bound gathers.
@@ -730,6 +739,18 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
             launch_weights_tapmajor(w3, f3, L2, (int)m, c->st) != cudaSuccess || cudaStreamSynchronize(c->st) != cudaSuccess) {
             delete c;
             return fail(DYN_ERR_CUDA, "FP32 weight copies failed");
+        }
+        if (d.mixed == 2) {
+            float2 *l1, *l2, *l3;
+            if ((s = dalloc(&l1, planes * L2)) || (s = dalloc(&l2, planes * L2)) || (s = dalloc(&l3, planes * L2))) { delete c; return s; }
+            d.wA1l = l1; d.wA2l = l2; d.wB2l = l3;
+            if (launch_weights_tapmajor_lo(w1, l1, L2, (int)m, c->st) != cudaSuccess ||
+                launch_weights_tapmajor_lo(w2, l2, L2, (int)m, c->st) != cudaSuccess ||
+                launch_weights_tapmajor_lo(w3, l3, L2, (int)m, c->st) != cudaSuccess ||
+                cudaStreamSynchronize(c->st) != cudaSuccess) {
+                delete c;
+                return fail(DYN_ERR_CUDA, "FP32 weight low parts failed");
+            }
         }
     }
     if (cudaMallocHost((void**)&c->stages_h, sizeof(StageDev) * SMAX) != cudaSuccess ||

@@ -246,13 +246,18 @@ __device__ void adapt_step(const Quench& q, Plan& pl, const TabDev& tb) {
 #ifndef DYN_BATCH_SHIFT
 #define DYN_BATCH_SHIFT 0
 #endif
-template <int M, int K, int P, int P2, int TPB>
-__global__ void __launch_bounds__(TPB, (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
+#ifndef DYN_BATCH_DF_TPSM
+#define DYN_BATCH_DF_TPSM 512
+#endif
+// DF: the (hi, lo) form (mdf::chunk): twice the staged row, more registers.
+template <int M, int K, int P, int P2, int TPB, bool DF = false>
+__global__ void __launch_bounds__(TPB, DF ? DYN_BATCH_DF_TPSM / TPB : (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
     k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,
                    const unsigned nitems, Work* work) {
     wait_prior_grid();
     extern __shared__ float2 s_lastf[];
     __shared__ mixed::RowShared sh;
+    __shared__ float s_clo[4];
     __shared__ unsigned s_item[2];  // the item being worked on and the next one
     constexpr int GMAX = mixed::RED_CAP / (8 * (TPB / 32));  // chunks per fold
     int p = 0;
@@ -267,13 +272,21 @@ __global__ void __launch_bounds__(TPB, (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
         if (pl.status == DYN_QUENCH_RUNNING) {
             const int i = (int)(e & 0xffffu);
             const StageDev& sp = q.stg[pl.sidx * SMAX + pl.s];
-            mixed::row_setup(q.c, sp, i, true, s_lastf, sh);
+            float2* s_lo = s_lastf + (q.c.L + 2);
+            if constexpr (DF) {
+                mixed::row_setup(q.c, sp, i, true, s_lastf, sh, s_clo);
+                mdf::stage_lo(q.c, sp, s_lo);
+            } else {
+                mixed::row_setup(q.c, sp, i, true, s_lastf, sh);
+            }
             __syncthreads();
             const int nch = q.c.nch;
             for (int ch0 = 0; ch0 < nch; ch0 += GMAX) {
                 const int ng = min(GMAX, nch - ch0);
-                for (int g = 0; g < ng; ++g)
-                    mixed::chunk_sums<M, K, P, P2, DYN_BATCH_SHIFT != 0>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
+                for (int g = 0; g < ng; ++g) {
+                    if constexpr (DF) mdf::chunk<M, K, P, P2>(q.c, sp, ch0 + g, g, s_lastf, s_lo, s_clo, sh, i);
+                    else mixed::chunk_sums<M, K, P, P2, DYN_BATCH_SHIFT != 0>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
+                }
                 __syncthreads();
                 mixed::fold_chunks(q.c, i, nch, ch0, ng, sh);
                 if (ch0 + GMAX < nch) __syncthreads();
@@ -358,6 +371,7 @@ struct GridDev {
     float* integ_f = nullptr;
     int* iA[3] = {nullptr, nullptr, nullptr};
     float2* wf[3] = {nullptr, nullptr, nullptr};  // tap-major FP32 pair planes
+    float2* wl[3] = {nullptr, nullptr, nullptr};  // their low parts (DYN_MIXED_DF)
 };
 
 struct Batch {
@@ -382,6 +396,7 @@ struct Batch {
     Work* work = nullptr;
     int tpb = 128, kpt = 1, ctas = 0;
     int M = 10, pp = 0;  // template selectors: stencil depth, (p, p2) kind
+    bool df = false;     // DYN_MIXED_DF: (hi, lo) inputs (mdf::chunk)
     size_t smem = 0, Lmax = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_ticks = 0;
@@ -407,6 +422,9 @@ struct Batch {
 
     template <int M_, int K_, int P_, int P2_, int TPB_>
     cudaError_t gather_t() {
+        if (df)  // the (hi, lo) form runs one target per thread
+            return launch_pdl(k_batch_gather<M_, 1, P_, P2_, TPB_, true>, dim3(nsm * ctas), dim3(TPB_), smem, st,
+                              (const Quench*)qd, (const Plan*)pd, (const unsigned*)items, nitems, work);
         return launch_pdl(k_batch_gather<M_, K_, P_, P2_, TPB_>, dim3(nsm * ctas), dim3(TPB_), smem, st,
                           (const Quench*)qd, (const Plan*)pd, (const unsigned*)items, nitems, work);
     }
@@ -433,8 +451,10 @@ struct Batch {
     int occupancy(int threads, int targets) {
         int nb = 0;
         const void* f;
-#define OCC_T(M_, K_, P_, P2_) \
-    (threads == 256 ? (const void*)k_batch_gather<M_, K_, P_, P2_, 256> : (const void*)k_batch_gather<M_, K_, P_, P2_, 128>)
+#define OCC_T(M_, K_, P_, P2_)                                                                        \
+    (df ? (threads == 256 ? (const void*)k_batch_gather<M_, 1, P_, P2_, 256, true>                        \
+                          : (const void*)k_batch_gather<M_, 1, P_, P2_, 128, true>)                       \
+        : (threads == 256 ? (const void*)k_batch_gather<M_, K_, P_, P2_, 256> : (const void*)k_batch_gather<M_, K_, P_, P2_, 128>))
 #define OCC_SEL(P_, P2_) \
     f = M == 10 ? (targets == 2 ? OCC_T(10, 2, P_, P2_) : OCC_T(10, 1, P_, P2_)) \
                 : (targets == 2 ? OCC_T(0, 2, P_, P2_) : OCC_T(0, 1, P_, P2_))
@@ -448,6 +468,7 @@ struct Batch {
     dyn_status set_tile(int threads, int targets, int ctas_per_sm) {
         if (threads != 128 && threads != 256) return bfail(DYN_ERR_INVALID, "threads must be 128 or 256");
         if (targets != 1 && targets != 2) return bfail(DYN_ERR_INVALID, "targets must be 1 or 2");
+        if (df) targets = 1;
         tpb = threads;
         kpt = targets;
         const int occ = occupancy(threads, targets);
@@ -543,6 +564,7 @@ struct Batch {
             cudaMemcpyAsync(q.c.inv_dtr, inv.data(), k * sizeof(double), cudaMemcpyHostToDevice, st) == cudaSuccess &&
             launch_mirror_rows(q.c.KR, q.c.KRf, k * L, st) == cudaSuccess &&
             launch_mirror_rows(q.c.dKR, q.c.dKRf, k * L, st) == cudaSuccess &&
+            (!q.c.KRl || launch_mirror_lo(q.c.KR, q.c.KRl, k * L, st) == cudaSuccess) &&
             launch_time_f32(q.c.t1grid, q.c.dtr, (int)k, q.c.inv_len_f, q.c.inv_dtr_f, st) == cudaSuccess;
         e = cudaStreamSynchronize(st);  // the host vectors above are sources of the copies
         release();
@@ -632,6 +654,7 @@ struct Batch {
         BCK(launch_rstep_exact(q.c, 1, q.c.drvec, st));
         BCK(launch_mirror_rows(q.c.KR, q.c.KRf, L, st));
         BCK(launch_mirror_rows(q.c.dKR, q.c.dKRf, L, st));
+        if (q.c.KRl) BCK(launch_mirror_lo(q.c.KR, q.c.KRl, L, st));
         Plan p{};
         p.status = DYN_QUENCH_RUNNING;
         p.n = 1;
@@ -679,8 +702,11 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         if (!(q.T0 > 0) || !(q.delta_t_min > 0) || !(q.delta_max > 0)) return bfail(DYN_ERR_INVALID, "T0, delta_t_min and delta_max must be positive");
         if (q.capacity != 0 && q.capacity < 2) return bfail(DYN_ERR_INVALID, "capacity must be at least 2 rows");
     }
+    if (cfg->precision != 0 && cfg->precision != DYN_MIXED && cfg->precision != DYN_MIXED_DF)
+        return bfail(DYN_ERR_INVALID, "batch precision: DYN_MIXED or DYN_MIXED_DF");
     Batch* bt = new Batch();
     bt->cfg = *cfg;
+    bt->df = cfg->precision == DYN_MIXED_DF;
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e != cudaSuccess) { delete bt; return bfail(DYN_ERR_CUDA, cudaGetErrorString(e)); }
     if (cfg->stream) {
@@ -731,6 +757,14 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
                     wt[(d >> 1) * L2 + tg] =
                         make_float2((float)w[k][tg * m + d], d + 1 < m ? (float)w[k][tg * m + d + 1] : 0.0f);
             BUP(gd.wf[k], wt.data(), planes * L2 * sizeof(float2));
+            if (bt->df) {
+                if ((s = bt->alloc(&gd.wl[k], planes * L2))) { delete bt; return s; }
+                auto lo = [](double v) { return (float)(v - (double)(float)v); };
+                for (size_t tg = 0; tg < L2; ++tg)
+                    for (size_t d = 0; d < m; d += 2)
+                        wt[(d >> 1) * L2 + tg] = make_float2(lo(w[k][tg * m + d]), d + 1 < m ? lo(w[k][tg * m + d + 1]) : 0.0f);
+                BUP(gd.wl[k], wt.data(), planes * L2 * sizeof(float2));
+            }
         }
     }
     bt->M = all10 ? 10 : 0;
@@ -741,7 +775,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         pp = pp < 0 ? k : (pp == k ? pp : 0);
     }
     bt->pp = pp;
-    bt->smem = (bt->Lmax + 2) * sizeof(float2);
+    bt->smem = (bt->df ? 2 : 1) * (bt->Lmax + 2) * sizeof(float2);
 
     // ---- tableaux
     {
@@ -777,7 +811,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         d.L = (int)L;
         d.m = (int)gd.m;
         d.search = cfg->search;
-        d.mixed = 1;
+        d.mixed = bt->df ? 2 : 1;
         d.M = make_model(sq.p, sq.p2, sq.lambda, sq.T0, sq.Gamma);
         d.theta = gd.theta;
         d.phi2 = gd.phi2;
@@ -789,6 +823,9 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         d.wA1f = gd.wf[0];
         d.wA2f = gd.wf[1];
         d.wB2f = gd.wf[2];
+        d.wA1l = gd.wl[0];
+        d.wA2l = gd.wl[1];
+        d.wB2l = gd.wl[2];
         const size_t G = (L + EPI_ROWS - 1) / EPI_ROWS, nchm = (L + nch_max_of - 1) / nch_max_of;
         if ((s = bt->alloc(&d.KR, cap * L)) || (s = bt->alloc(&d.dKR, cap * L)) ||
             (s = bt->alloc(&d.KRf, cap * L + 16)) || (s = bt->alloc(&d.dKRf, cap * L + 16)) ||
@@ -802,6 +839,10 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
             (s = bt->alloc(&q.stg, 2 * SMAX))) {
             delete bt;
             return s;
+        }
+        if (bt->df) {
+            if ((s = bt->alloc(&d.KRl, cap * L + 16))) { delete bt; return s; }
+            cudaMemset(d.KRl, 0, (cap * L + 16) * sizeof(float2));
         }
         // the 16-byte segment loads may touch one element past the last row
         cudaMemset(d.KRf, 0, (cap * L + 16) * sizeof(float2));
@@ -897,6 +938,7 @@ dyn_status dyn_batch_upload(void* p, int qi, const dyn_state* stt, const dyn_con
     BCK(cudaMemcpyAsync(q.c.inv_dtr, inv.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
     BCK(launch_mirror_rows(q.c.KR, q.c.KRf, n * L, st));
     BCK(launch_mirror_rows(q.c.dKR, q.c.dKRf, n * L, st));
+    if (q.c.KRl) BCK(launch_mirror_lo(q.c.KR, q.c.KRl, n * L, st));
     BCK(launch_time_f32(q.c.t1grid, q.c.dtr, (int)n, q.c.inv_len_f, q.c.inv_dtr_f, st));
     Plan pl{};
     pl.status = DYN_QUENCH_RUNNING;
@@ -1076,6 +1118,7 @@ dyn_status dyn_batch_tune(void* p, int reps, int* threads, int* targets, int* ct
     dyn_status s;
     for (int t : {128, 256}) {
         for (int k : {1, 2}) {
+            if (bt->df && k == 2) continue;
             const int occ = bt->occupancy(t, k);
             std::vector<int> cands = {occ};
             if (occ >= 4) cands.push_back(occ / 2);

@@ -214,6 +214,9 @@ __device__ __forceinline__ void rows(const DevCtx& c, const StageDev& sp, const 
             c.dKR[(size_t)sp.n0 * L + i] = make_double2(td * h0.x, td * h0.y);
             if constexpr (MIXED) {
                 c.KRf[(size_t)sp.n0 * L + i] = make_float2((float)g.x, (float)g.y);
+                if (c.KRl)
+                    c.KRl[(size_t)sp.n0 * L + i] =
+                        make_float2((float)(g.x - (double)(float)g.x), (float)(g.y - (double)(float)g.y));
                 c.dKRf[(size_t)sp.n0 * L + i] = make_float2((float)(td * h0.x), (float)(td * h0.y));
             }
             // rstep (time_steps.cpp:83-92) of the new row at its time

@@ -59,7 +59,7 @@ struct GatherRec {
 
 struct DevCtx {
     int L, m, nch, search, kpt, tpb;
-    int mixed;             // 1: FP32 gathers/convolutions (dyn_mixed.cu)
+    int mixed;             // 1: FP32 gathers/convolutions (dyn_mixed.cu); 2: with (hi, lo) inputs
     DModel M;
     const double* theta;
     const double* phi2;
@@ -99,6 +99,10 @@ struct DevCtx {
     const float2* wB2f;
     float2* KRf;
     float2* dKRf;
+    float2* KRl;           // mixed 2: low parts of (QK, QR), KR - (double)KRf
+    const float2* wA1l;    // mixed 2: low parts of the FP32 weights (same layout as wA1f)
+    const float2* wA2l;
+    const float2* wB2l;
     const float* integ_f;  // [L]   int.dat in FP32
     float* inv_dtr_f;      // [cap] 1/delta_t_ratio in FP32
     float* inv_len_f;      // [cap] 1/(t1grid[k+1]-t1grid[k]) in FP32
@@ -211,6 +215,8 @@ cudaError_t launch_pack_rows(const double* QK, const double* QR, double2* out, s
                              cudaStream_t st);
 cudaError_t launch_main_mixed(const DevCtx& c, int s, cudaStream_t st);
 cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cudaStream_t st);
+cudaError_t launch_mirror_lo(const double2* in, float2* out, size_t count, cudaStream_t st);
+cudaError_t launch_weights_tapmajor_lo(const double* in, float2* out, size_t targets, int m, cudaStream_t st);
 cudaError_t launch_weights_f32(const double* in, float* out, size_t count, cudaStream_t st);
 // [L*L][m] FP64 stencil rows to the tap-major FP32 pair planes of the mixed form
 cudaError_t launch_weights_tapmajor(const double* in, float2* out, size_t targets, int m, cudaStream_t st);

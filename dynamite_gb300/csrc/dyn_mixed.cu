@@ -33,10 +33,36 @@ __global__ void __launch_bounds__(128, K == 1 ? 10 : 4) k_main_mixed(const DevCt
     mixed::fold_chunks(c, i, gridDim.x, blockIdx.x, 1, sh);
 }
 
+
+// The (hi, lo) form of k_main_mixed (device functions in dyn_mixed.cuh, namespace mdf)
+template <int M, int K, int P, int P2>
+__global__ void __launch_bounds__(128, K == 1 ? 8 : 4) k_main_df(const DevCtx c, const int s) {
+    wait_prior_grid();
+    const StageDev& sp = c.stages[s];
+    extern __shared__ float2 s_row[];  // [L+2] hi, [L+2] lo of the last history row
+    __shared__ mixed::RowShared sh;
+    __shared__ float s_clo[4];
+    const int i = blockIdx.y;
+    float2* s_lo = s_row + (c.L + 2);
+    mixed::row_setup(c, sp, i, blockIdx.x == 0, s_row, sh, s_clo);
+    mdf::stage_lo(c, sp, s_lo);
+    __syncthreads();
+    mdf::chunk<M, K, P, P2>(c, sp, blockIdx.x, 0, s_row, s_lo, s_clo, sh, i);
+    __syncthreads();
+    mixed::fold_chunks(c, i, gridDim.x, blockIdx.x, 1, sh);
+}
+
 namespace {
 
 template <int M, int K, int P, int P2>
+cudaError_t launch_df(const DevCtx& c, int s, cudaStream_t st) {
+    dim3 grid(c.nch, c.L), block(c.tpb);
+    return launch_pdl(k_main_df<M, K, P, P2>, grid, block, 2 * (size_t)(c.L + 2) * sizeof(float2), st, c, s);
+}
+
+template <int M, int K, int P, int P2>
 cudaError_t launch_t(const DevCtx& c, int s, cudaStream_t st) {
+    if (c.mixed == 2) return launch_df<M, K, P, P2>(c, s, st);
     dim3 grid(c.nch, c.L), block(c.tpb);
     return launch_pdl(k_main_mixed<M, K, P, P2>, grid, block, (size_t)(c.L + 2) * sizeof(float2), st, c, s);
 }
@@ -63,6 +89,14 @@ __global__ void k_to_f32(const double2* in, float2* out, size_t count) {
     }
 }
 
+// low parts: v - (double)(float)v
+__global__ void k_to_f32_lo(const double2* in, float2* out, size_t count) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = in[e];
+        out[e] = make_float2((float)(v.x - (double)(float)v.x), (float)(v.y - (double)(float)v.y));
+    }
+}
+
 // FP32 inverse interval lengths and inverse step ratios of rows [0, n)
 __global__ void k_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -76,12 +110,14 @@ __global__ void k_weights_f32(const double* in, float* out, size_t count) {
         out[e] = (float)in[e];
 }
 
-// out[p][e] = (w[e][2p], w[e][2p+1]) in FP32 (second tap 0 past the depth)
+// out[p][e] = (w[e][2p], w[e][2p+1]) in FP32 (second tap 0 past the depth);
+// with LO the low parts w - (double)(float)w instead
+template <bool LO>
 __global__ void k_weights_tapmajor(const double* in, float2* out, size_t targets, int m) {
+    auto part = [](double w) { return LO ? (float)(w - (double)(float)w) : (float)w; };
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < targets; e += (size_t)gridDim.x * blockDim.x)
         for (int d = 0; d < m; d += 2)
-            out[(size_t)(d >> 1) * targets + e] =
-                make_float2((float)in[e * m + d], d + 1 < m ? (float)in[e * m + d + 1] : 0.0f);
+            out[(size_t)(d >> 1) * targets + e] = make_float2(part(in[e * m + d]), d + 1 < m ? part(in[e * m + d + 1]) : 0.0f);
 }
 
 }  // namespace
@@ -106,7 +142,19 @@ cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* i
 
 cudaError_t launch_weights_tapmajor(const double* in, float2* out, size_t targets, int m, cudaStream_t st) {
     const int blocks = (int)((targets + 255) / 256 < 8192 ? (targets + 255) / 256 : 8192);
-    k_weights_tapmajor<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, targets, m);
+    k_weights_tapmajor<false><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, targets, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weights_tapmajor_lo(const double* in, float2* out, size_t targets, int m, cudaStream_t st) {
+    const int blocks = (int)((targets + 255) / 256 < 8192 ? (targets + 255) / 256 : 8192);
+    k_weights_tapmajor<true><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, targets, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mirror_lo(const double2* in, float2* out, size_t count, cudaStream_t st) {
+    const int blocks = (int)((count + 255) / 256 < 8192 ? (count + 255) / 256 : 8192);
+    k_to_f32_lo<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, count);
     return cudaGetLastError();
 }
 

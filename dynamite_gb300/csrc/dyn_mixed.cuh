@@ -268,7 +268,7 @@ struct RowShared {
 // position.  A stage flagged `fresh` searches the row's B1 position itself
 // (after a rollback) instead of reading the one the previous stage left.
 __device__ __forceinline__ void row_setup(const DevCtx& c, const StageDev& sp, const int i, const bool first,
-                                          float2* s_lastf, RowShared& sh) {
+                                          float2* s_lastf, RowShared& sh, float* clo = nullptr) {
     const int L = c.L, tpb = blockDim.x;
     const int nrows = sp.nrows;
     const double t = sp.T;
@@ -292,6 +292,10 @@ __device__ __forceinline__ void row_setup(const DevCtx& c, const StageDev& sp, c
                 c0 = 1.0 - u2; c1 = u2; c2 = u + u2; c3 = 0.0;
             }
             sh.c[0] = (float)c0; sh.c[1] = (float)c1; sh.c[2] = (float)c2; sh.c[3] = (float)c3;
+            if (clo) {
+                clo[0] = (float)(c0 - (double)sh.c[0]); clo[1] = (float)(c1 - (double)sh.c[1]);
+                clo[2] = (float)(c2 - (double)sh.c[2]); clo[3] = (float)(c3 - (double)sh.c[3]);
+            }
             sh.bi[0] = (int)F; sh.bi[1] = cubic;
             if (first) {
                 const double2 x0 = c.KR[(size_t)(F - 1) * L], x1 = c.KR[(size_t)F * L];
@@ -307,6 +311,7 @@ __device__ __forceinline__ void row_setup(const DevCtx& c, const StageDev& sp, c
         } else {
             sh.bi[0] = 1; sh.bi[1] = 0;
             sh.c[0] = sh.c[1] = sh.c[2] = sh.c[3] = 0.f;
+            if (clo) clo[0] = clo[1] = clo[2] = clo[3] = 0.f;
             if (first) c.rowval[i] = make_double2(c.KR[0].x, c.rvec[0]);
         }
         if (i == 0 && first) c.slots->q0 = c.KR[(size_t)(nrows - 1) * L].x;
@@ -477,4 +482,238 @@ __device__ __forceinline__ void fold_chunks(const DevCtx& c, const int i, const 
 }
 
 }  // namespace mixed
+
+// ---------------------------------------------------------------- (hi, lo) form
+// Plain FP32 gathers go wrong over long runs through FP32 roundings that repeat
+// step after step (the rounded weights and stored history, and the rounding of
+// sums over them).  Here the weights and the stored (QK, QR) history carry FP32
+// (hi, lo) pairs; the A1/A2 and B2 stencil sums form every term as an exact
+// FP32 product plus the cross terms (w_hi x_lo + w_lo x_hi) and add them with
+// TwoSum; each gathered value is rounded once to FP32 for Sigma and the
+// convolution products.  B1 combines old rows with coefficients that move with
+// t: plain products with the low parts as cross terms suffice there.  The
+// derivative rows (dQK, dQR), a step's worth of change, stay single FP32.
+namespace mdf {
+using namespace mixed;
+
+// (s, c) += (wh + wl) * (xh + xl)
+__device__ __forceinline__ void add_prod(float& s, float& c, float wh, float wl, float xh, float xl) {
+    const float p = wh * xh;
+    float e = fmaf(wh, xh, -p);
+    e = fmaf(wh, xl, e);
+    e = fmaf(wl, xh, e);
+    const float t = s + p, bp = t - s;
+    c += ((s - (t - bp)) + (p - bp)) + e;
+    s = t;
+}
+
+// sum_d w[d] * x[d] over the m taps of target ij for both components, as
+// (s_QK, c_QK, s_QR, c_QR); weights from the tap-major (hi, lo) planes, the
+// segment x from the (hi, lo) history arrays (global or shared)
+template <int M>
+__device__ __forceinline__ float4 gather(const float2* __restrict__ wh, const float2* __restrict__ wl, size_t L2,
+                                         size_t ij, const float2* xh, const float2* xl, int m, bool ldg) {
+    float sx = 0.f, cx = 0.f, sy = 0.f, cy = 0.f;
+    const int mm = M > 0 ? M : m;
+#pragma unroll
+    for (int d = 0; d < (M > 0 ? M : 1 << 20); d += 2) {
+        if (d >= mm) break;
+        const float2 ph = __ldg(wh + (size_t)(d >> 1) * L2 + ij), pl = __ldg(wl + (size_t)(d >> 1) * L2 + ij);
+        const float2 ah = ldg ? __ldg(xh + d) : xh[d], al = ldg ? __ldg(xl + d) : xl[d];
+        add_prod(sx, cx, ph.x, pl.x, ah.x, al.x);
+        add_prod(sy, cy, ph.x, pl.x, ah.y, al.y);
+        if (d + 1 < mm) {
+            const float2 bh = ldg ? __ldg(xh + d + 1) : xh[d + 1], bl = ldg ? __ldg(xl + d + 1) : xl[d + 1];
+            add_prod(sx, cx, ph.y, pl.y, bh.x, bl.x);
+            add_prod(sy, cy, ph.y, pl.y, bh.y, bl.y);
+        }
+    }
+    return make_float4(sx, cx, sy, cy);
+}
+
+// The depth-10 gather with the (hi, lo) history read as six 16-byte loads per
+// array from the even element at or below the start b (the seg10 layout),
+// weights wh/wl already in registers; taps in order.
+template <bool LDG>
+__device__ __forceinline__ float4 gather10(const float wh[10], const float wl[10], const float2* xh, const float2* xl,
+                                           size_t b) {
+    const size_t a = b & ~(size_t)1;
+    const bool sh = b & 1;
+    const float4* ph = reinterpret_cast<const float4*>(xh + a);
+    const float4* pl = reinterpret_cast<const float4*>(xl + a);
+    float sx = 0.f, cx = 0.f, sy = 0.f, cy = 0.f;
+    float2 hprev = make_float2(0.f, 0.f), lprev = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float4 vh = LDG ? __ldg(ph + k) : ph[k];
+        const float4 vl = LDG ? __ldg(pl + k) : pl[k];
+        // elements 2k, 2k+1 of the window; tap d reads element d + (b & 1)
+        const float2 h0 = make_float2(vh.x, vh.y), h1 = make_float2(vh.z, vh.w);
+        const float2 l0 = make_float2(vl.x, vl.y), l1 = make_float2(vl.z, vl.w);
+        if (k >= 1) {
+            const int d = 2 * k - 1;
+            const float2 xh_ = sh ? h0 : hprev, xl_ = sh ? l0 : lprev;
+            add_prod(sx, cx, wh[d], wl[d], xh_.x, xl_.x);
+            add_prod(sy, cy, wh[d], wl[d], xh_.y, xl_.y);
+        }
+        if (k <= 4) {
+            const int d = 2 * k;
+            const float2 xh_ = sh ? h1 : h0, xl_ = sh ? l1 : l0;
+            add_prod(sx, cx, wh[d], wl[d], xh_.x, xl_.x);
+            add_prod(sy, cy, wh[d], wl[d], xh_.y, xl_.y);
+        }
+        hprev = h1;
+        lprev = l1;
+    }
+    return make_float4(sx, cx, sy, cy);
+}
+
+__device__ __forceinline__ void load_w10_hl(const float2* __restrict__ wh, const float2* __restrict__ wl, size_t L2,
+                                            size_t ij, float h[10], float l[10]) {
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+        const float2 a = __ldg(wh + d * L2 + ij), b = __ldg(wl + d * L2 + ij);
+        h[2 * d] = a.x; h[2 * d + 1] = a.y;
+        l[2 * d] = b.x; l[2 * d + 1] = b.y;
+    }
+}
+
+// One chunk of tpb*K targets of row i in the (hi, lo) form (as chunk_sums);
+// s_hi / s_lo: the staged last row, clo: low parts of the B1 coefficients.
+template <int M, int K, int P, int P2>
+__device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const int ch, const int slot,
+                                      const float2* s_hi, const float2* s_lo, const float* clo, RowShared& sh,
+                                      const int i) {
+    const int L = c.L, tpb = blockDim.x;
+    const size_t L2 = (size_t)L * L;
+    const int nrows = sp.nrows;
+    const double t = sp.T;
+    const bool live = t > 0.0;
+    const FModel Mf{c.M.p, c.M.p2, (float)c.M.cA, (float)c.M.cB, (float)c.M.cC, (float)c.M.cD};
+    const int m = M > 0 ? M : c.m;
+    const float bh0 = sh.c[0], bh1 = sh.c[1], bh2 = sh.c[2], bh3 = sh.c[3];
+    const float bl0 = clo[0], bl1 = clo[1];
+    const int F = sh.bi[0], cubic1 = sh.bi[1];
+    const int maxX = sp.maxX;
+    const float2 fill = c.KRf[0];
+    const ListView lv{c.t1grid, nrows, t};
+    float acc[8], cmp[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { acc[k] = 0.f; cmp[k] = 0.f; }
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+        const int j = ch * tpb * K + kk * tpb + threadIdx.x;
+        if (j < L) {
+            const size_t ij = (size_t)i * L + j;
+            float2 a1, a2, b1, b2;
+            if (live) {
+                {
+                    const int s1 = __ldg(c.iA1 + ij), s2 = __ldg(c.iA2 + ij);
+                    float4 g1, g2;
+                    if constexpr (M == 10) {
+                        float wh[10], wl[10];
+                        load_w10_hl(c.wA1f, c.wA1l, L2, ij, wh, wl);
+                        g1 = gather10<false>(wh, wl, s_hi, s_lo, (size_t)s1);
+                        load_w10_hl(c.wA2f, c.wA2l, L2, ij, wh, wl);
+                        g2 = gather10<false>(wh, wl, s_hi, s_lo, (size_t)s2);
+                    } else {
+                        g1 = gather<M>(c.wA1f, c.wA1l, L2, ij, s_hi + s1, s_lo + s1, m, false);
+                        g2 = gather<M>(c.wA2f, c.wA2l, L2, ij, s_hi + s2, s_lo + s2, m, false);
+                    }
+                    a1 = make_float2(g1.x + g1.y, g1.z + g1.w);
+                    a2 = make_float2(g2.x + g2.y, g2.z + g2.w);
+                }
+                {
+                    const size_t r0 = (size_t)(F - 1) * L + j, r1 = (size_t)F * L + j;
+                    const float2 x0 = __ldg(c.KRf + r0), x0l = __ldg(c.KRl + r0);
+                    const float2 x1 = __ldg(c.KRf + r1), x1l = __ldg(c.KRl + r1);
+                    const float2 d1 = __ldg(c.dKRf + r1);
+                    // the coefficients move with t, so plain FP32 products suffice once the
+                    // rows' low parts and c0, c1's low parts enter as cross terms
+                    const float2 d2 = cubic1 ? __ldg(c.dKRf + (size_t)(F + 1) * L + j) : make_float2(0.f, 0.f);
+                    b1.x = bh0 * x0.x + (bl0 * x0.x + bh0 * x0l.x + bh1 * x1l.x + bl1 * x1.x - bh2 * d1.x - bh3 * d2.x) +
+                           bh1 * x1.x;
+                    b1.y = bh0 * x0.y + (bl0 * x0.y + bh0 * x0l.y + bh1 * x1l.y + bl1 * x1.y - bh2 * d1.y - bh3 * d2.y) +
+                           bh1 * x1.y;
+                }
+                {
+                    int X;
+                    float x;
+                    pos_split(lv, c.inv_len_f, __dmul_rn(__ldg(c.phi2 + ij), t), X, x);
+                    if (X > maxX) { x += __int2float_rn(X - maxX); X = maxX; }
+                    if (X < 1) { x -= __int2float_rn(1 - X); X = 1; }
+                    const float x2 = x * x, x3 = x2 * x;
+                    const size_t base = (size_t)(X - 1) * (size_t)L + (size_t)__ldg(c.iB2 + ij);
+                    const bool cubic2 = X < nrows - 1;
+                    float4 S0, S1;
+                    float2 D1, D2 = make_float2(0.f, 0.f);
+                    if constexpr (M == 10) {
+                        // even L (the M == 10 kernels require it): every row segment has base's parity
+                        float wh[10], wl[10];
+                        load_w10_hl(c.wB2f, c.wB2l, L2, ij, wh, wl);
+                        S0 = gather10<true>(wh, wl, c.KRf, c.KRl, base);
+                        S1 = gather10<true>(wh, wl, c.KRf, c.KRl, base + L);
+                        D1 = seg10(wh, c.dKRf, base + L);
+                        if (cubic2) D2 = seg10(wh, c.dKRf, base + 2 * L);
+                    } else {
+                        S0 = gather<M>(c.wB2f, c.wB2l, L2, ij, c.KRf + base, c.KRl + base, m, true);
+                        S1 = gather<M>(c.wB2f, c.wB2l, L2, ij, c.KRf + base + L, c.KRl + base + L, m, true);
+                        D1 = dotfT(c.wB2f, L2, ij, c.dKRf + base + L, m, true);
+                        if (cubic2) D2 = dotfT(c.wB2f, L2, ij, c.dKRf + base + 2 * L, m, true);
+                    }
+                    // S0 + e2 (S1 - S0) + e1 D1 + e3 D2 (e0 = 1 - e2): the FP32 Hermite
+                    // weights only scale the row difference
+                    float e1, e2, e3;
+                    if (cubic2) {
+                        e1 = x - 2.f * x2 + x3;
+                        e2 = 3.f * x2 - 2.f * x3;
+                        e3 = (x3 - x2) * __ldg(c.inv_dtr_f + X + 1);
+                    } else {
+                        e1 = x - x2;
+                        e2 = x2;
+                        e3 = 0.f;
+                    }
+                    const float dSx = (S1.x - S0.x) + (S1.y - S0.y), dSy = (S1.z - S0.z) + (S1.w - S0.w);
+                    b2.x = S0.x + (S0.y + (e2 * dSx + e1 * D1.x + e3 * D2.x));
+                    b2.y = S0.z + (S0.w + (e2 * dSy + e1 * D1.y + e3 * D2.y));
+                }
+            } else {
+                a1 = a2 = b1 = b2 = fill;
+            }
+            float sKA1, dA1, sKB1, dB1, sKB2, dB2;
+            SigF<P, P2>::d12(Mf, a1.x, sKA1, dA1);
+            const float sRA1 = dA1 * a1.y;
+            const float sRA2 = SigF<P, P2>::d2(Mf, a2.x) * a2.y;
+            SigF<P, P2>::d12(Mf, b1.x, sKB1, dB1);
+            const float sRB1 = dB1 * b1.y;
+            SigF<P, P2>::d12(Mf, b2.x, sKB2, dB2);
+            const float sRB2 = dB2 * b2.y;
+            const float wj = __ldg(c.integ_f + j);
+            const float wRA2 = wj * sRA2, wQRA2 = wj * a2.y;
+            const float v[8] = {wRA2 * b2.x, (wj * sRA1) * b1.x, (wj * sKA1) * b1.y, wQRA2 * sKB2,
+                                (wj * a1.y) * sKB1, (wj * a1.x) * sRB1, wRA2 * b2.y, wQRA2 * sRB2};
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (kk == 0) acc[k] = v[k];
+                else two_sum_add(acc[k], cmp[k], v[k]);
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float H, Lo;
+    warp_reduce8_pair(acc, cmp, lane, H, Lo);
+    if ((lane & 3) == 0) sh.red[((slot * (tpb >> 5)) + warp) * 8 + warp_reduce8_index(lane)] = make_float2(H, Lo);
+}
+
+// The low parts of the last history row into shared memory (after row_setup
+// staged the high parts)
+__device__ __forceinline__ void stage_lo(const DevCtx& c, const StageDev& sp, float2* s_lo) {
+    const int L = c.L;
+    const float2* KRl = c.KRl + (size_t)(sp.nrows - 1) * L;
+    for (int k = threadIdx.x; k < L; k += blockDim.x) s_lo[k] = KRl[k];
+    if (threadIdx.x == 0) s_lo[L] = make_float2(0.f, 0.f), s_lo[L + 1] = make_float2(0.f, 0.f);
+}
+
+}  // namespace mdf
+
 }  // namespace dyn

@@ -57,7 +57,8 @@ def synthetic_history(grid: Grid, n: int, T: float = 0.6, t_lo: float = 1e-5, t_
     return State(t, dtr, QK.ravel(), QR.ravel(), dQK.ravel(), dQR.ravel(), np.ones(n), np.zeros(n))
 
 
-def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5, tmax: float = 0.0) -> dict:
+def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5, tmax: float = 0.0,
+                precision: str = "mixed") -> dict:
     """Mixed form against the FP64 form on the FP64 run's step schedule (see module doc);
     with tmax > 0 the FP64 run stops at t >= tmax (nsteps is then a cap)."""
     import time
@@ -66,7 +67,7 @@ def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5, tmax:
     L = grid.L
     m = Model(p=3, p2=4, lam=lam, Gamma=T)
     a = Simulation(grid, m, history_capacity=nsteps + 64)
-    b = Simulation(grid, m, precision="mixed", history_capacity=nsteps + 64)
+    b = Simulation(grid, m, precision=precision, history_capacity=nsteps + 64)
     a.init()
     b.init()
     t0 = time.perf_counter()
@@ -88,7 +89,8 @@ def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5, tmax:
     c_a, c_b = float(w @ QA[-1]), float(w @ QB[-1])
     r_a, r_b = float(w @ RA[-1]), float(w @ RB[-1])
     rel = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
-    return {"form": "mixed_error", "L": L, "steps": nsteps, "t_final": float(t[-1]), "T": T, "lam": lam,
+    return {"form": "mixed_error", "precision": precision, "L": L, "steps": nsteps, "t_final": float(t[-1]),
+            "T": T, "lam": lam,
             "history_rows": int(t.size), "s_fp64": t1 - t0, "s_mixed": t2 - t1,
             "time_grid_identical": bool(np.array_equal(sa.t1grid, sb.t1grid)),
             "energy": rel(tb["energy"], ta["energy"]), "r": rel(sb.rvec, sa.rvec), "C_history": rel(QB, QA),
@@ -96,7 +98,8 @@ def mixed_error(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5, tmax:
             "C_tf_half_tf": abs(c_b - c_a) / abs(c_a), "R_tf_tf_half": abs(r_b - r_a) / abs(r_a)}
 
 
-def long_run(grid: Grid, nmax: int, tmax: float, T: float = 0.6, lam: float = 0.5, every: int = 100000) -> dict:
+def long_run(grid: Grid, nmax: int, tmax: float, T: float = 0.6, lam: float = 0.5, every: int = 100000,
+             precision: str = "mixed") -> dict:
     """FP64 run to tmax with the periodic sparsify, then the mixed form on its schedule."""
     import time
     from .grid import lagrange_weights
@@ -106,7 +109,7 @@ def long_run(grid: Grid, nmax: int, tmax: float, T: float = 0.6, lam: float = 0.
     w = lagrange_weights(grid.theta, 0.5)
     out = {"form": "long", "L": L, "tmax": tmax, "T": T, "lam": lam, "sparsify_every": every}
     sched = None
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", precision):
         s = Simulation(grid, m, precision=prec, history_capacity=min(nmax, every) + 64)
         s.init()
         t0 = time.perf_counter()
@@ -123,7 +126,7 @@ def long_run(grid: Grid, nmax: int, tmax: float, T: float = 0.6, lam: float = 0.
                      "t_final": float(st.t1grid[-1]), "history_rows": int(st.t1grid.size), "energy": s.energy(),
                      "r": float(st.rvec[-1]), "C_tf_half_tf": float(w @ last_K), "R_tf_tf_half": float(w @ last_R)}
         s.close()
-    a, b = out["fp64"], out["mixed"]
+    a, b = out["fp64"], out[precision]
     out["mixed_rel_err"] = {k: abs(b[k] - a[k]) / abs(a[k]) for k in ("energy", "r", "C_tf_half_tf", "R_tf_tf_half")}
     return out
 
@@ -133,6 +136,8 @@ def main(argv=None):
     ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error", "long"], default="batch")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--tmax", type=float, default=0.0, help="mixed_error: run the FP64 form to t >= tmax")
+    ap.add_argument("--precision", choices=["mixed", "mixed_df"], default="mixed",
+                    help="mixed_error / long / fp64 stage timing: the mixed form to compare")
     ap.add_argument("--L", type=int, default=512)
     ap.add_argument("--rows", type=int, default=4096)
     ap.add_argument("--quenches", type=int, default=16)
@@ -156,16 +161,17 @@ def main(argv=None):
                           "dE_dT": float(g[0]), "dE_dlam": float(g[1]), **stats}))
         return
     if a.form == "long":
-        print(json.dumps(long_run(grid, a.steps, a.tmax, a.T)))
+        print(json.dumps(long_run(grid, a.steps, a.tmax, a.T, precision=a.precision)))
         return
     if a.form == "mixed_error":
-        print(json.dumps(mixed_error(grid, a.steps, a.T, tmax=a.tmax)))
+        print(json.dumps(mixed_error(grid, a.steps, a.T, tmax=a.tmax, precision=a.precision)))
         return
     st = synthetic_history(grid, a.rows, a.T)
     t = st.t1grid
     out = {"form": a.form, "L": a.L, "rows": a.rows}
     if a.form in ("fp64", "mixed"):
-        s = Simulation(grid, Model(p=3, p2=4, lam=0.5, Gamma=a.T), precision=a.form, history_capacity=a.rows + 2)
+        prec = a.form if a.form == "fp64" else a.precision
+        s = Simulation(grid, Model(p=3, p2=4, lam=0.5, Gamma=a.T), precision=prec, history_capacity=a.rows + 2)
         s.upload(st)
         ms_main, ms_epi = s.profile_stage(reps=a.reps)
         out.update(ms_main=ms_main, ms_epilogue=ms_epi)
@@ -173,10 +179,10 @@ def main(argv=None):
     else:
         qs = [Quench(grid=0, p=3, p2=4, lam=(0.3, 0.5, 0.7)[b % 3], Gamma=0.4 + 0.6 * b / max(a.quenches - 1, 1),
                      capacity=a.rows + 2) for b in range(a.quenches)]
-        bt = Batch([grid], qs)
+        bt = Batch([grid], qs, precision=a.precision)
         for q in range(a.quenches):
             bt.upload(q, st, delta_t=0.01 * (t[-1] - t[-2]), method=1)
-        out.update(quenches=a.quenches, ms_gather=bt.profile(reps=a.reps))
+        out.update(quenches=a.quenches, precision=a.precision, ms_gather=bt.profile(reps=a.reps))
         bt.close()
     print(json.dumps(out))
 

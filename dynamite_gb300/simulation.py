@@ -90,7 +90,7 @@ class Simulation:
         self.L = grid.L
         self._h = C.c_void_p()
         cfg = _lib.Config(model.p, model.p2, model.lam, model.T0, model.Gamma, grid.L, grid.depth,
-                          model.delta_t_min, model.delta_max, {"fp64": 0, "mixed": 1}[precision],
+                          model.delta_t_min, model.delta_max, {"fp64": 0, "mixed": 1, "mixed_df": 2}[precision],
                           SEARCH[search], history_capacity, device, stream, int(use_graph))
         self._keep = [np.ascontiguousarray(a) for a in (grid.theta, grid.phi2, grid.integ)]
         i64 = [np.ascontiguousarray(a, dtype=np.int64) for a in (grid.indsA1, grid.indsA2, grid.indsB2)]

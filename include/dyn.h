@@ -43,7 +43,11 @@ enum {
 };
 
 /* Arithmetic of the O(L^2) gathers and reductions. */
-enum { DYN_FP64 = 0, DYN_MIXED = 1 };
+/* DYN_MIXED_DF: the mixed form with its frozen inputs carried as FP32 (hi, lo)
+ * pairs (stencil weights, the history mirror, the B1 coefficients) and the
+ * gathers summed as exact FP32 products with compensated sums; the rest as
+ * DYN_MIXED. */
+enum { DYN_FP64 = 0, DYN_MIXED = 1, DYN_MIXED_DF = 2 };
 
 /* Fractional-position search in t1grid. */
 enum {
@@ -78,7 +82,7 @@ typedef struct {
     size_t depth;           /* stencil depth m (interp order + 1) */
     double delta_t_min;
     double delta_max;
-    int precision;          /* DYN_FP64 | DYN_MIXED */
+    int precision;          /* DYN_FP64 | DYN_MIXED | DYN_MIXED_DF */
     int search;             /* DYN_SEARCH_* */
     size_t history_capacity;/* rows to preallocate (0: default) */
     int device;             /* CUDA device ordinal */
@@ -303,6 +307,7 @@ typedef struct {
     long long sparsify_every;
     int sparsify_sweeps;
     int sparsify_variant;
+    int precision;           /* DYN_MIXED (or 0) | DYN_MIXED_DF */
 } dyn_batch_config;
 
 /* Quench status */

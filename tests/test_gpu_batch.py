@@ -168,3 +168,18 @@ def test_batch_periodic_sparsify_equals_single(product_built):
             assert (inf["delta_t"], inf["method"], inf["loop"]) == (c["delta_t"], c["method"], c["loop"])
             assert inf["energy"] == tr["energy"][-1]
         b.close()
+
+
+def test_batch_df_equals_single_df(product_built):
+    """The (hi, lo) form in a batch: every quench equals the same quench run alone in that form."""
+    grids, m32, m64 = _grids()
+    specs = [(0, m32, 50), (1, m64, 35)]
+    b = D.Batch(grids, [_quench(gi, m, max_steps=n) for gi, m, n in specs], ticks_per_launch=16, precision="mixed_df")
+    b.run(100_000)
+    for q, (gi, m, n) in enumerate(specs):
+        s = D.Simulation(grids[gi], m, precision="mixed_df")
+        s.init()
+        tr = s.run(n)
+        _assert_same_state(b.download(q), s.download())
+        assert b.info(q)["energy"] == tr["energy"][-1]
+    b.close()

@@ -71,3 +71,35 @@ def test_mixed_sparsify_and_graph_replay(product_built):
     r1 = s.update(1, dt)
     r2 = s.update(1, dt)
     assert np.isfinite([r1.delta, r2.delta, r2.energy]).all()
+
+
+MIXED_DF_TOL = 1e-8   # (hi, lo) inputs: the frozen FP32 roundings removed
+
+
+@pytest.mark.parametrize("L", [32, 64])
+def test_mixed_df_trajectory_vs_reference(product_built, L):
+    g = load_golden(L)
+    s = D.Simulation(grid_from(g, D.Grid), model_from(g, D.Model), precision="mixed_df")
+    s.init()
+    tr = s.run(g["traj_dt"].size, schedule=(g["traj_dt"], g["traj_method"]))
+    st = s.download()
+    np.testing.assert_array_equal(st.t1grid, g["traj_final_t1grid"])
+    assert rel_err(tr["energy"], g["traj_energy"]) < MIXED_DF_TOL
+    assert rel_err(st.QK, g["traj_final_QK"]) < MIXED_DF_TOL
+    assert rel_err(st.rvec, g["traj_final_rvec"]) < MIXED_DF_TOL
+
+
+def test_mixed_df_large_grid_vs_fp64(product_built):
+    """L=512, 300 steps of the FP64 run's schedule in the (hi, lo) form."""
+    grid = D.grid.generate(512)
+    m = D.Model(p=3, p2=4, lam=0.5, Gamma=0.6)
+    a = D.Simulation(grid, m)
+    b = D.Simulation(grid, m, precision="mixed_df")
+    a.init()
+    b.init()
+    ta = a.run(300)
+    tb = b.run(300, schedule=(ta["dt"], ta["method"]))
+    sa, sb = a.download(), b.download()
+    assert rel_err(tb["energy"], ta["energy"]) < MIXED_DF_TOL
+    assert rel_err(sb.QK, sa.QK) < MIXED_DF_TOL
+    assert rel_err(sb.QR, sa.QR) < MIXED_DF_TOL
