@@ -247,9 +247,11 @@ __device__ void adapt_step(const Quench& q, Plan& pl, const TabDev& tb) {
 #define DYN_BATCH_SHIFT 0
 #endif
 #ifndef DYN_BATCH_DF_TPSM
-#define DYN_BATCH_DF_TPSM 512
+#define DYN_BATCH_DF_TPSM 1024
 #endif
-// DF: the (hi, lo) form (mdf::chunk): twice the staged row, more registers.
+// DF: the (hi, lo) form (mdf::chunk): twice the staged row; its cap of 64
+// registers (DYN_BATCH_DF_TPSM = 1024 threads per SM) spills a little but beats
+// 128 registers at 512 threads (1.58 vs 1.80 ms for 64 quenches at L=512).
 template <int M, int K, int P, int P2, int TPB, bool DF = false>
 __global__ void __launch_bounds__(TPB, DF ? DYN_BATCH_DF_TPSM / TPB : (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
     k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,

@@ -135,6 +135,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error", "long"], default="batch")
     ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--tune", action="store_true", help="batch: autotune the gather tile first")
     ap.add_argument("--tmax", type=float, default=0.0, help="mixed_error: run the FP64 form to t >= tmax")
     ap.add_argument("--precision", choices=["mixed", "mixed_df"], default="mixed",
                     help="mixed_error / long / fp64 stage timing: the mixed form to compare")
@@ -182,6 +183,8 @@ def main(argv=None):
         bt = Batch([grid], qs, precision=a.precision)
         for q in range(a.quenches):
             bt.upload(q, st, delta_t=0.01 * (t[-1] - t[-2]), method=1)
+        if a.tune:
+            out.update(tile=bt.tune(reps=3))
         out.update(quenches=a.quenches, precision=a.precision, ms_gather=bt.profile(reps=a.reps))
         bt.close()
     print(json.dumps(out))
