@@ -219,7 +219,7 @@ def test_rollback(product_built):
 
 @pytest.mark.parametrize("L", [128, 512])
 def test_fixed_schedule_large_grid(product_built, L):
-    """BASELINE-sized grids (poly-9, Tmax 1e5): GPU vs the oracle (binary
+    """Production-sized grids (poly-9, Tmax 1e5): GPU vs the oracle (binary
     search, the CUDA path's positions) over a short run from t = 0."""
     grid = D.grid.generate(L)
     m = D.Model(p=3, p2=4, lam=0.5, Gamma=0.6)
