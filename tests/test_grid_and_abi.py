@@ -72,3 +72,12 @@ def test_invalid_arguments_rejected_without_touching_the_gpu(product_built):
     assert b"null" in L.dyn_last_error()
     assert L.dyn_update(None, 1, 1e-3, None) == -1
     assert L.dyn_sparsify(None, 1e-10, 0, None) == -1
+
+
+def test_missing_library_raises(monkeypatch, tmp_path):
+    """No fallback: without the native library every numeric call fails loudly."""
+    from dynamite_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "absent.so"))
+    with pytest.raises(_lib.DynError):
+        _lib.lib()
