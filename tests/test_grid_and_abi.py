@@ -81,3 +81,27 @@ def test_missing_library_raises(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "absent.so"))
     with pytest.raises(_lib.DynError):
         _lib.lib()
+
+
+def test_batch_and_adjoint_arguments_rejected_without_touching_the_gpu(product_built):
+    """Bad batch configurations and quenches, and adjoint calls on a null context, fail
+    with DYN_ERR_INVALID before any CUDA call."""
+    D = product_built
+    from dynamite_gb300 import _lib
+    g = D.grid.generate(32)
+    for bad in (dict(p=1), dict(grid=3), dict(delta_max=0.0), dict(capacity=1)):
+        with pytest.raises(_lib.DynError):
+            D.Batch([g], [D.Quench(**bad)])
+    with pytest.raises(KeyError):
+        D.Batch([g], [D.Quench()], precision="fp64")       # batches run the mixed forms only
+    # a sparsify variant out of range, through the C ABI
+    cfg = _lib.BatchConfig(0, None, 0, 0, 32, 128, 1, 0, 100, 1, 7, 1)
+    qs = (_lib.BatchQuench * 1)(_lib.BatchQuench(0, 3, 4, 0.5, 1e50, 0.6, 1e-5, 1e-10, 0.0, 0.0, 0, 64))
+    gs = (_lib.BatchGrid * 1)()
+    h = C.c_void_p()
+    L = D.lib()
+    assert L.dyn_batch_create(C.byref(cfg), gs, 1, qs, 1, C.byref(h)) == -1
+    assert b"sparsify variant" in L.dyn_last_error()
+    assert L.dyn_adjoint_forward(None, None, None) == -1
+    assert L.dyn_adjoint_backward(None, None, None, None) == -1
+    assert L.dyn_batch_run(None, 1, None) == -1
