@@ -247,11 +247,12 @@ __device__ void adapt_step(const Quench& q, Plan& pl, const TabDev& tb) {
 #define DYN_BATCH_SHIFT 0
 #endif
 #ifndef DYN_BATCH_DF_TPSM
-#define DYN_BATCH_DF_TPSM 1024
+#define DYN_BATCH_DF_TPSM 1152
 #endif
-// DF: the (hi, lo) form (mdf::chunk): twice the staged row; its cap of 64
-// registers (DYN_BATCH_DF_TPSM = 1024 threads per SM) spills a little but beats
-// 128 registers at 512 threads (1.58 vs 1.80 ms for 64 quenches at L=512).
+// DF: the (hi, lo) form (mdf::chunk): twice the staged row; its cap of 56
+// registers (DYN_BATCH_DF_TPSM = 1152 threads per SM) spills but beats 128
+// registers at 512 threads: 1.53 vs 1.80 ms for 64 quenches at L=512 (64
+// registers: 1.57, 72: 1.64, 48: 1.77).
 template <int M, int K, int P, int P2, int TPB, bool DF = false>
 __global__ void __launch_bounds__(TPB, DF ? DYN_BATCH_DF_TPSM / TPB : (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
     k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,
