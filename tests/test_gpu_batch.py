@@ -19,8 +19,8 @@ def _quench(grid_idx, m: D.Model, **kw):
                     delta_max=m.delta_max, **kw)
 
 
-def _single(grid, m: D.Model, nsteps, rollback=False, tmax=0.0, upload=None, ctl=None):
-    s = D.Simulation(grid, m, precision="mixed")
+def _single(grid, m: D.Model, nsteps, rollback=False, tmax=0.0, upload=None, ctl=None, precision="mixed"):
+    s = D.Simulation(grid, m, precision=precision)
     if upload is None:
         s.init()
     else:
@@ -107,16 +107,17 @@ def test_batch_rollback_matches_single(product_built):
     assert b.info(0)["n"] < 81  # some steps were rolled back
 
 
-def test_batch_upload_continues_like_single(product_built):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_batch_upload_continues_like_single(product_built, precision):
     g = load_golden(32)
     grids, m32, _ = _grids()
     mid = state_from(g, "mid", D.State)
     ctl = dict(delta_t=float(mid.t1grid[-1] - mid.t1grid[-2]), method=1, delta=1e-11, delta_old=2e-11, loop=40)
-    b = D.Batch(grids, [_quench(0, m32, max_steps=5), _quench(1, m32, max_steps=5)])
+    b = D.Batch(grids, [_quench(0, m32, max_steps=5), _quench(1, m32, max_steps=5)], precision=precision)
     b.upload(0, mid, **ctl)
     b.set_limits(0, max_steps=30)
     b.run(100_000)
-    s, _ = _single(grids[0], m32, 30, upload=mid, ctl=ctl)
+    s, _ = _single(grids[0], m32, 30, upload=mid, ctl=ctl, precision=precision)
     _assert_same_state(b.download(0), s.download())
 
 
@@ -139,7 +140,8 @@ def test_batch_autotuned_tiles(product_built):
         assert abs(b.info(q)["energy"] - tr["energy"][-1]) <= MIXED_TRAJ_TOL * abs(tr["energy"][-1])
 
 
-def test_batch_periodic_sparsify_equals_single(product_built):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_batch_periodic_sparsify_equals_single(product_built, precision):
     """The reference driver's periodic sparsify (every 20 loops here) inside a batch: each
     quench pauses at the end of the loop, the host compacts its history, the controller
     and planner resume on the device; the result equals dyn_run with the same cadence."""
@@ -153,12 +155,12 @@ def test_batch_periodic_sparsify_equals_single(product_built):
     specs = [(0, m, 70), (1, m2, 45)]
     for variant in ("gpu", "cpu"):
         b = D.Batch(grids, [_quench(gi, mm, max_steps=n) for gi, mm, n in specs], ticks_per_launch=16,
-                    sparsify_every=20, sparsify_variant=variant)
+                    sparsify_every=20, sparsify_variant=variant, precision=precision)
         b.run(100_000)
         for q, (gi, mm, n) in enumerate(specs):
             inf = b.info(q)
             assert inf["status"] == "max_steps" and inf["steps"] == n
-            s = D.Simulation(grids[gi], mm, precision="mixed")
+            s = D.Simulation(grids[gi], mm, precision=precision)
             s.init()
             tr = s.run(n, sparsify_every=20, sparsify_variant=variant)
             st = s.download()
