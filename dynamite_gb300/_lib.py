@@ -140,6 +140,7 @@ def lib():
         vp = C.c_void_p
         sigs = {
             "dyn_abi_version": ([], C.c_int),
+            "dyn_energy_history": ([vp, dp, C.c_size_t], C.c_int),
             "dyn_last_error": ([], C.c_char_p),
             "dyn_ctx_create": ([C.POINTER(Config), C.POINTER(Tables), C.POINTER(vp)], C.c_int),
             "dyn_ctx_destroy": ([vp], C.c_int),

@@ -998,6 +998,20 @@ dyn_status dyn_energy(void* p, double* e) {
     return DYN_OK;
 }
 
+dyn_status dyn_energy_history(void* p, double* e, size_t n_rows) {
+    if (!p || !e) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (n_rows != c->n) return fail(DYN_ERR_INVALID, "n_rows must equal the history rows");
+    double* buf;
+    if (dalloc(&buf, n_rows)) return DYN_ERR_NOMEM;
+    cudaError_t err = launch_energy_history(c->d, (int)n_rows, buf, c->st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(e, buf, n_rows * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(c->st);
+    cudaFree(buf);
+    CK(err);
+    return DYN_OK;
+}
+
 dyn_status dyn_conv_dev(void* p, int kind, const double* f, const double* g, size_t n, double t, double* out) {
     if (!p || !f || !g || !out) return fail(DYN_ERR_INVALID, "null argument");
     Ctx* c = C(p);

@@ -719,4 +719,34 @@ cudaError_t launch_unpack_rows(const double2* in, double* QK, double* QR, size_t
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------------
+// Energy of every history row as the reference writes it at save time
+// (computeEnergyHistoryKernel, io_output.cu:61-122):
+//   E_k = -t_k (sum_j w_j f'(QK[k,j]) QR[k,j] + f'(QK[k,0]) / T0)
+// (the T0 term carries the factor t_k there, unlike energyGPU's per-step E).
+// One warp per row, lanes over the columns, a shuffle sum.
+__global__ void k_energy_history(const DevCtx c, const int nrows, double* out) {
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k >= nrows) return;  // whole warps: k is uniform over a warp
+    const int L = c.L;
+    const double2* row = c.KR + (size_t)k * L;
+    double sum = 0.0;
+    for (int j = lane; j < L; j += 32) {
+        const double2 v = row[j];
+        const double sk = Df_x(c.M, v.x);
+        sum = fma(sk * v.y, c.integ[j], sum);
+        if (j == 0) sum += sk / c.M.T0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) out[k] = -c.t1grid[k] * sum;
+}
+
+cudaError_t launch_energy_history(const DevCtx& c, int nrows, double* out, cudaStream_t st) {
+    if (nrows <= 0) return cudaSuccess;
+    k_energy_history<<<(nrows + 7) / 8, 256, 0, st>>>(c, nrows, out);
+    return cudaGetLastError();
+}
+
 }  // namespace dyn

@@ -202,6 +202,7 @@ cudaError_t launch_drstep2_exact(const DevCtx& c, const double* qK, const double
                                  const double* dqK, const double* dqR, double t, double* out,
                                  cudaStream_t st);
 cudaError_t launch_energy_exact(const DevCtx& c, int nrows, double* out, cudaStream_t st);
+cudaError_t launch_energy_history(const DevCtx& c, int nrows, double* out, cudaStream_t st);
 cudaError_t launch_conv_exact(const DevCtx& c, int kind, const double* f, const double* g,
                               size_t n, double t, double* out, cudaStream_t st);
 cudaError_t launch_search(const DevCtx& c, const double* list, size_t nlist, const double* elem,

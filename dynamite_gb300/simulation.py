@@ -195,6 +195,12 @@ class Simulation:
         _lib.check(_lib.lib().dyn_energy(self._h, C.byref(v)), "dyn_energy")
         return v.value
 
+    def energy_history(self) -> np.ndarray:
+        """E at every history row as RG-Evo writes it with a save (io_output.cu:61-122)."""
+        out = np.empty(self.n)
+        _lib.check(_lib.lib().dyn_energy_history(self._h, _lib.ptr(out), out.size), "dyn_energy_history")
+        return out
+
     def update(self, method: int | None = None, delta_t: float | None = None) -> StepResult:
         c = self.controller
         m = c["method"] if method is None else method

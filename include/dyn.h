@@ -198,6 +198,10 @@ dyn_status dyn_rstep(void* ctx, double* r);
 dyn_status dyn_drstep2(void* ctx, const double* qK, const double* qR, const double* dqK,
                        const double* dqR, double t, double* dr);
 dyn_status dyn_energy(void* ctx, double* e);
+/* The energy of every history row as RG-Evo writes it with a save
+ * (computeEnergyHistoryKernel, io_output.cu:61-122), into host e[n_rows]:
+ * E_k = -t_k (sum_j w_j f'(QK[k,j]) QR[k,j] + f'(QK[k,0]) / T0). */
+dyn_status dyn_energy_history(void* ctx, double* e, size_t n_rows);
 /* ConvAGPU / ConvRGPU (convolution.cu:64-230): kind 0 = A, 1 = R; f, g,
  * out are device arrays, n = len (1-D) or len*len (2-D). */
 dyn_status dyn_conv_dev(void* ctx, int kind, const double* f, const double* g, size_t n, double t,

@@ -341,3 +341,21 @@ def test_checkpoint_resume_continues_bit_for_bit(product_built, tmp_path):
     sa, sb = a.download(), b.download()
     for k in ("t1grid", "QK", "QR", "dQK", "dQR", "rvec", "drvec"):
         np.testing.assert_array_equal(getattr(sa, k), getattr(sb, k), err_msg=k)
+
+
+def test_energy_history_as_the_reference_saves_it(product_built):
+    """computeEnergyHistoryKernel (io_output.cu:61-122) restated in numpy: E_k = -t_k (sum_j
+    w_j f'(QK[k,j]) QR[k,j] + f'(QK[k,0]) / T0) over every row of a mid-run history."""
+    g = load_golden(32)
+    s = sim_for(g)
+    st = state_from(g, "traj_final", D.State)
+    s.upload(st)
+    e = s.energy_history()
+    m = model_from(g, D.Model)
+    L = 32
+    QK, QR = st.QK.reshape(-1, L), st.QR.reshape(-1, L)
+    fp = lambda q: m.lam * m.p * q ** (m.p - 1) + (1 - m.lam) * m.p2 * q ** (m.p2 - 1)
+    w = g["grid_integ"]
+    ref = -st.t1grid * ((fp(QK) * QR * w[None, :]).sum(axis=1) + fp(QK[:, 0]) / m.T0)
+    assert e.shape == ref.shape
+    assert np.max(np.abs(e - ref)) <= 1e-13 * np.max(np.abs(ref))
