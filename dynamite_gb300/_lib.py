@@ -30,7 +30,7 @@ class Config(C.Structure):
         ("p", C.c_int), ("p2", C.c_int), ("lam", C.c_double), ("T0", C.c_double), ("Gamma", C.c_double),
         ("len", C.c_size_t), ("depth", C.c_size_t), ("delta_t_min", C.c_double), ("delta_max", C.c_double),
         ("precision", C.c_int), ("search", C.c_int), ("history_capacity", C.c_size_t), ("device", C.c_int),
-        ("stream", C.c_void_p), ("use_graph", C.c_int),
+        ("stream", C.c_void_p), ("use_graph", C.c_int), ("log_response", C.c_int),
     ]
 
 

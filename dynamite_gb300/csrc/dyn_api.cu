@@ -661,6 +661,9 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     if (L < 4 || L > 4096 || m < 2 || m > L) return fail(DYN_ERR_INVALID, "len must be in [4, 4096] and 2 <= depth <= len");
     if (cfg->precision != DYN_FP64 && cfg->precision != DYN_MIXED && cfg->precision != DYN_MIXED_DF)
         return fail(DYN_ERR_INVALID, "unknown precision");
+    if (cfg->log_response != 0 && cfg->log_response != 1) return fail(DYN_ERR_INVALID, "log_response must be 0 or 1");
+    if (cfg->log_response && cfg->precision != DYN_FP64)
+        return fail(DYN_ERR_UNSUPPORTED, "log-space response runs on the FP64 form");
     const size_t L2 = L * L;
     std::vector<int> i32[3];
     {
@@ -686,6 +689,7 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     d.L = (int)L;
     d.m = (int)m;
     d.search = cfg->search;
+    d.logr = cfg->log_response;
     d.mixed = cfg->precision == DYN_MIXED ? 1 : cfg->precision == DYN_MIXED_DF ? 2 : 0;
     // tile shape: threads per CTA x targets per thread.  FP64: few wide CTAs
     // amortize the FP64 reduction; mixed: one target per thread keeps more
@@ -1210,6 +1214,7 @@ dyn_status dyn_adjoint_forward(void* p, const dyn_run_params* rp, dyn_step_resul
     if (!p || !rp) return fail(DYN_ERR_INVALID, "null argument");
     Ctx* c = C(p);
     if (c->d.mixed) return fail(DYN_ERR_UNSUPPORTED, "the adjoint runs on the FP64 form");
+    if (c->d.logr) return fail(DYN_ERR_UNSUPPORTED, "the adjoint differentiates the linear-domain gathers only");
     if (rp->gpu_rollback || rp->sparsify_every > 0)
         return fail(DYN_ERR_INVALID, "the adjoint needs an append-only history: no rollback, no sparsify");
     if (c->n == 0) return fail(DYN_ERR_STATE, "no state: call dyn_state_init or dyn_state_upload");

@@ -34,8 +34,46 @@ __device__ __forceinline__ void next_position(const DevCtx& c, const StageDev& s
 }
 
 // ------------------------------------------------------------------------
+// Log-space response (the reference's -R option).  QK is interpolated as in
+// the linear form; QR is interpolated as f = log QR with the derivatives
+// g = dQR / QR and exponentiated, wherever every value it rests on is
+// positive, and linearly otherwise.
+
+// A1/A2 (index_vec.cu:185-226): lx holds log QR of the last row (QR itself
+// where QR <= 0, as the reference's log slice does, index_vec.cu:367-375)
+template <int M>
+__device__ __forceinline__ double2 dot2s_log(const double* __restrict__ w, const double2* x, const double* lx, int m) {
+    double qk = 0.0, qr = 0.0, sl = 0.0;
+    bool ok = true;
+    const int n = M > 0 ? M : m;
+#pragma unroll
+    for (int d = 0; d < n; ++d) {
+        const double ww = __ldg(w + d);
+        const double2 v = x[d];
+        qk = fma(ww, v.x, qk);
+        qr = fma(ww, v.y, qr);
+        sl = fma(ww, lx[d], sl);
+        ok = ok && v.y > 0.0;
+    }
+    return make_double2(qk, ok ? exp(sl) : qr);
+}
+
+// B1 (index_vec.cu:456-530) with the row's coefficients: r0, r1 the QR nodes,
+// g1, g2 the stored dQR at the nodes' right neighbours; c3 = 0 on the
+// quadratic branch
+__device__ __forceinline__ double b1_log(double c0, double c1, double c2, double c3, double r0, double r1, double g1,
+                                         double g2, double lin) {
+    if (!(r0 > 0.0 && r1 > 0.0)) return lin;
+    double f = c0 * log(r0) + c1 * log(r1) - c2 * (g1 / r0);
+    if (c3 != 0.0) f -= c3 * (g2 / r1);
+    return exp(f);
+}
+
+// ------------------------------------------------------------------------
 // k_main: fused gathers + Sigma + convolution products for one stage.
-template <int M, int K, int P, int P2>
+// LOGR: QR gathers in log space (the last row's logs staged after it in
+// shared memory).
+template <int M, int K, int P, int P2, bool LOGR = false>
 __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
     wait_prior_grid();
     const StageDev& sp = c.stages[s];
@@ -48,8 +86,14 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
     __shared__ int s_bi[2];
     __shared__ double s_red[4][8];
 
+    double* s_logR = reinterpret_cast<double*>(s_last + L);  // LOGR only: [L]
+
     const double2* KRl = c.KR + (size_t)(nrows - 1) * L;
-    for (int k = threadIdx.x; k < L; k += tpb) s_last[k] = KRl[k];
+    for (int k = threadIdx.x; k < L; k += tpb) {
+        const double2 v = KRl[k];
+        s_last[k] = v;
+        if constexpr (LOGR) s_logR[k] = v.y > 0.0 ? log(v.y) : v.y;
+    }
     if (threadIdx.x == 0) {
         if (live) {
             const B1Row r = b1_row(c, c.posB1x[i], sp.maxceil, nrows);
@@ -100,19 +144,27 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
             const size_t ij = (size_t)i * L + j;
             double2 a1, a2, b1, b2;
             if (live) {
-                a1 = dot2s<M>(c.wA1 + ij * m, s_last + __ldg(c.iA1 + ij), m);
-                a2 = dot2s<M>(c.wA2 + ij * m, s_last + __ldg(c.iA2 + ij), m);
+                if constexpr (LOGR) {
+                    const int ia1 = __ldg(c.iA1 + ij), ia2 = __ldg(c.iA2 + ij);
+                    a1 = dot2s_log<M>(c.wA1 + ij * m, s_last + ia1, s_logR + ia1, m);
+                    a2 = dot2s_log<M>(c.wA2 + ij * m, s_last + ia2, s_logR + ia2, m);
+                } else {
+                    a1 = dot2s<M>(c.wA1 + ij * m, s_last + __ldg(c.iA1 + ij), m);
+                    a2 = dot2s<M>(c.wA2 + ij * m, s_last + __ldg(c.iA2 + ij), m);
+                }
                 {
                     const double2 x0 = __ldg(c.KR + (size_t)(F - 1) * L + j);
                     const double2 x1 = __ldg(c.KR + (size_t)F * L + j);
                     const double2 d1 = __ldg(c.dKR + (size_t)F * L + j);
                     b1.x = bc0 * x0.x + bc1 * x1.x - bc2 * d1.x;
                     b1.y = bc0 * x0.y + bc1 * x1.y - bc2 * d1.y;
+                    double2 d2 = make_double2(0.0, 0.0);
                     if (cubic1) {
-                        const double2 d2 = __ldg(c.dKR + (size_t)(F + 1) * L + j);
+                        d2 = __ldg(c.dKR + (size_t)(F + 1) * L + j);
                         b1.x -= bc3 * d2.x;
                         b1.y -= bc3 * d2.y;
                     }
+                    if constexpr (LOGR) b1.y = b1_log(bc0, bc1, bc2, cubic1 ? bc3 : 0.0, x0.y, x1.y, d1.y, d2.y, b1.y);
                 }
                 {
                     double pos2;
@@ -137,10 +189,15 @@ __global__ void __launch_bounds__(128) k_main(const DevCtx c, const int s) {
                         const double e3 = (x3 - x2) * c.inv_dtr[X + 1];
                         b2.x = e0 * S0.x + e1 * D1.x + e2 * S1.x + e3 * D2.x;
                         b2.y = e0 * S0.y + e1 * D1.y + e2 * S1.y + e3 * D2.y;
+                        // index_mat.cu:203-212: Hermite of log of the row sums
+                        if (LOGR && S0.y > 0.0 && S1.y > 0.0)
+                            b2.y = exp(e0 * log(S0.y) + e1 * (D1.y / S0.y) + e2 * log(S1.y) + e3 * (D2.y / S1.y));
                     } else {
                         const double e0 = 1.0 - x2, e2 = x - x2;
                         b2.x = e0 * S0.x + x2 * S1.x + e2 * D1.x;
                         b2.y = e0 * S0.y + x2 * S1.y + e2 * D1.y;
+                        if (LOGR && S0.y > 0.0 && S1.y > 0.0)  // index_mat.cu:216-222
+                            b2.y = exp(e0 * log(S0.y) + x2 * log(S1.y) + e2 * (D1.y / S0.y));
                     }
                     if (c.rec) c.rec[ij] = GatherRec{a1, a2, b1, b2, x, (int)X, 0};
                 }
@@ -233,6 +290,20 @@ __device__ __forceinline__ double ip_exact(const double* w, const double2* x, in
     return acc;
 }
 
+// exp(sum_d w_d log QR_d) when every QR_d > 0, else the linear value lin
+// (index_vec.cpp:24-57, whose CPU form sums the logs in long double; this sum,
+// like the reference's CUDA kernel index_vec.cu:185-226, is in double)
+__device__ __forceinline__ double ip_log_exact(const double* w, const double2* x, int m, double lin) {
+    double acc = 0.0;
+    bool ok = true;
+    for (int d = 0; d < m; ++d) {
+        const double v = x[d].y;
+        ok = ok && v > 0.0;
+        acc = add(acc, mul(w[d], v > 0.0 ? log(v) : v));
+    }
+    return ok ? exp(acc) : lin;
+}
+
 // posB1x (given or searched), Floor clamp, B2 clamp (interpolation_core.cpp:19-114)
 __global__ void k_pos_b1_exact(const DevCtx c, const int nrows, const double* pos1_given,
                                const double* pos2_given) {
@@ -284,6 +355,10 @@ __global__ void k_interp_exact(const DevCtx c, const int nrows, const double* po
             v[1] = ip_exact(w1, KRl + c.iA1[ij], m, 1);
             v[2] = ip_exact(w2, KRl + c.iA2[ij], m, 0);
             v[3] = ip_exact(w2, KRl + c.iA2[ij], m, 1);
+            if (c.logr) {  // index_vec.cpp:24-57
+                v[1] = ip_log_exact(w1, KRl + c.iA1[ij], m, v[1]);
+                v[3] = ip_log_exact(w2, KRl + c.iA2[ij], m, v[3]);
+            }
             // B1: index_vec.cpp:63-136
             {
                 const double pos = c.posB1x[i];
@@ -302,10 +377,15 @@ __global__ void k_interp_exact(const DevCtx c, const int nrows, const double* po
                     const double e3 = add(in3, in4);
                     v[4] = sub(sub(add(mul(e0, x0.x), mul(e1, x1.x)), mul(e2, d1.x)), dvd(mul(e3, d2.x), dr));
                     v[5] = sub(sub(add(mul(e0, x0.y), mul(e1, x1.y)), mul(e2, d1.y)), dvd(mul(e3, d2.y), dr));
+                    if (c.logr && x0.y > 0.0 && x1.y > 0.0)  // index_vec.cpp:89-100
+                        v[5] = exp(sub(sub(add(mul(e0, log(x0.y)), mul(e1, log(x1.y))), mul(e2, dvd(d1.y, x0.y))),
+                                       mul(dvd(e3, dr), dvd(d2.y, x1.y))));
                 } else {
                     const double e0 = sub(1.0, in3), e2 = add(wt, in3);
                     v[4] = add(sub(mul(e0, x0.x), mul(e2, d1.x)), mul(in3, x1.x));
                     v[5] = add(sub(mul(e0, x0.y), mul(e2, d1.y)), mul(in3, x1.y));
+                    if (c.logr && x0.y > 0.0 && x1.y > 0.0)  // index_vec.cpp:122-127
+                        v[5] = exp(sub(add(mul(e0, log(x0.y)), mul(in3, log(x1.y))), mul(e2, dvd(d1.y, x0.y))));
                 }
             }
             // B2: index_mat.cpp:18-91
@@ -328,8 +408,13 @@ __global__ void k_interp_exact(const DevCtx c, const int nrows, const double* po
                         const double e2 = sub(mul(3.0, x2), mul(2.0, x3));
                         const double e3 = add(-x2, x3);
                         val = add(add(add(mul(e0, S0), mul(e1, D1)), mul(e2, S1)), dvd(mul(e3, D2), c.dtr[X + 1]));
+                        if (comp == 1 && c.logr && S0 > 0.0 && S1 > 0.0)  // index_mat.cpp:47-58
+                            val = exp(add(add(add(mul(e0, log(S0)), mul(e1, dvd(D1, S0))), mul(e2, log(S1))),
+                                          mul(dvd(e3, c.dtr[X + 1]), dvd(D2, S1))));
                     } else {
                         val = add(add(mul(sub(1.0, x2), S0), mul(x2, S1)), mul(sub(x, x2), D1));
+                        if (comp == 1 && c.logr && S0 > 0.0 && S1 > 0.0)  // index_mat.cpp:76-82
+                            val = exp(add(add(mul(sub(1.0, x2), log(S0)), mul(x2, log(S1))), mul(sub(x, x2), dvd(D1, S0))));
                     }
                     v[6 + comp] = val;
                 }
@@ -575,25 +660,32 @@ __global__ void k_fp64_probe(double* out, int iters) {
 
 // ------------------------------------------------------------------------
 // launch wrappers
-template <int M, int K, int P, int P2>
+template <int M, int K, int P, int P2, bool LOGR>
 static cudaError_t launch_main_t(const DevCtx& c, int s, cudaStream_t st) {
     dim3 grid(c.nch, c.L), block(c.tpb);
-    const size_t smem = (size_t)c.L * sizeof(double2);
+    const size_t smem = (size_t)c.L * (LOGR ? sizeof(double2) + sizeof(double) : sizeof(double2));
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_main<M, K, P, P2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        cudaFuncSetAttribute(k_main<M, K, P, P2, LOGR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             LOGR ? 96 * 1024 : 64 * 1024);
         attr_set = true;
     }
-    return launch_pdl(k_main<M, K, P, P2>, grid, block, smem, st, c, s);
+    return launch_pdl(k_main<M, K, P, P2, LOGR>, grid, block, smem, st, c, s);
 }
 
+template <int M, int P, int P2, bool LOGR>
+static cudaError_t launch_main_kl(const DevCtx& c, int s, cudaStream_t st) {
+    switch (c.kpt) {
+        case 1: return launch_main_t<M, 1, P, P2, LOGR>(c, s, st);
+        case 2: return launch_main_t<M, 2, P, P2, LOGR>(c, s, st);
+        default: return launch_main_t<M, 4, P, P2, LOGR>(c, s, st);
+    }
+}
+
+// the log-space form is built once, on the generic-exponent model
 template <int M, int P, int P2>
 static cudaError_t launch_main_k(const DevCtx& c, int s, cudaStream_t st) {
-    switch (c.kpt) {
-        case 1: return launch_main_t<M, 1, P, P2>(c, s, st);
-        case 2: return launch_main_t<M, 2, P, P2>(c, s, st);
-        default: return launch_main_t<M, 4, P, P2>(c, s, st);
-    }
+    return c.logr ? launch_main_kl<M, -1, -1, true>(c, s, st) : launch_main_kl<M, P, P2, false>(c, s, st);
 }
 
 template <int P, int P2>

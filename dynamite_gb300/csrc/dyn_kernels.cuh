@@ -60,6 +60,7 @@ struct GatherRec {
 struct DevCtx {
     int L, m, nch, search, kpt, tpb;
     int mixed;             // 1: FP32 gathers/convolutions (dyn_mixed.cu); 2: with (hi, lo) inputs
+    int logr;              // 1: QR gathers in log space (FP64 form only)
     DModel M;
     const double* theta;
     const double* phi2;

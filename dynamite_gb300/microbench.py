@@ -144,6 +144,7 @@ def main(argv=None):
     ap.add_argument("--quenches", type=int, default=16)
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--T", type=float, default=0.6)
+    ap.add_argument("--log-response", action="store_true", help="fp64 stage timing: QR gathers in log space")
     a = ap.parse_args(argv)
     from . import build as B
     B.build()
@@ -172,10 +173,14 @@ def main(argv=None):
     out = {"form": a.form, "L": a.L, "rows": a.rows}
     if a.form in ("fp64", "mixed"):
         prec = a.form if a.form == "fp64" else a.precision
-        s = Simulation(grid, Model(p=3, p2=4, lam=0.5, Gamma=a.T), precision=prec, history_capacity=a.rows + 2)
+        logr = a.log_response and prec == "fp64"
+        s = Simulation(grid, Model(p=3, p2=4, lam=0.5, Gamma=a.T), precision=prec, history_capacity=a.rows + 2,
+                       log_response=logr)
+        if logr:  # QR > 0 everywhere, so the log-space branches run: QR -> -QR, dQR -> -dQR
+            st = State(st.t1grid, st.dtr, st.QK, -st.QR, st.dQK, -st.dQR, st.rvec, st.drvec)
         s.upload(st)
         ms_main, ms_epi = s.profile_stage(reps=a.reps)
-        out.update(ms_main=ms_main, ms_epilogue=ms_epi)
+        out.update(ms_main=ms_main, ms_epilogue=ms_epi, log_response=logr)
         s.close()
     else:
         qs = [Quench(grid=0, p=3, p2=4, lam=(0.3, 0.5, 0.7)[b % 3], Gamma=0.4 + 0.6 * b / max(a.quenches - 1, 1),

@@ -84,14 +84,15 @@ def serk2_method(q: int) -> int:
 
 class Simulation:
     def __init__(self, grid: Grid, model: Model, precision: str = "fp64", search: str = "binary",
-                 device: int = 0, use_graph: bool = True, history_capacity: int = 0, stream: int | None = None):
+                 device: int = 0, use_graph: bool = True, history_capacity: int = 0, stream: int | None = None,
+                 log_response: bool = False):
         self.grid = grid
         self.model = model
         self.L = grid.L
         self._h = C.c_void_p()
         cfg = _lib.Config(model.p, model.p2, model.lam, model.T0, model.Gamma, grid.L, grid.depth,
                           model.delta_t_min, model.delta_max, {"fp64": 0, "mixed": 1, "mixed_df": 2}[precision],
-                          SEARCH[search], history_capacity, device, stream, int(use_graph))
+                          SEARCH[search], history_capacity, device, stream, int(use_graph), int(log_response))
         self._keep = [np.ascontiguousarray(a) for a in (grid.theta, grid.phi2, grid.integ)]
         i64 = [np.ascontiguousarray(a, dtype=np.int64) for a in (grid.indsA1, grid.indsA2, grid.indsB2)]
         w = [np.ascontiguousarray(a, dtype=np.float64) for a in (grid.wA1, grid.wA2, grid.wB2)]

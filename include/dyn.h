@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DYN_ABI_VERSION 2
+#define DYN_ABI_VERSION 3
 
 typedef enum {
     DYN_OK = 0,
@@ -88,6 +88,8 @@ typedef struct {
     int device;             /* CUDA device ordinal */
     void* stream;           /* cudaStream_t to run on; NULL: the context creates one */
     int use_graph;          /* capture each RK step into a CUDA graph */
+    int log_response;       /* 1: QR gathers in log space, the reference's -R option (index_vec.cu:183-395,
+                               index_mat.cu:149-227); DYN_FP64 only, fused stage kernels only */
 } dyn_config;
 
 /* Grid tables as RG-Evo writes them (grid_cli.cpp:163-215, read back by

@@ -55,6 +55,10 @@ double text_round_trip(long double v) {
 
 extern "C" {
 
+// The -R option (config.cpp:164-166): QR gathered in log space by
+// indexVecLN3 / indexVecN / indexMatAll.  dynref_setup resets it to off.
+void dynref_set_log_response(int on) { config.log_response_interp = on != 0; }
+
 // Model / controller parameters (config.hpp:18-56).
 int dynref_setup(int p, int p2, double lambda, double T0, double Gamma, size_t len,
                  double delta_t_min, double delta_max, int nthreads) {

@@ -18,6 +18,13 @@ Cases (one .npz per grid size):
   traj_*     the reference controller run from t=0: per-step dt, method,
              error, time, energy, and the final history
   spars_*    sparsifyNscale (CPU-only build variant) of the trajectory state
+
+golden_log_L64.npz: the log-space response option (-R, config.log_response_interp)
+on the grid and model of golden_L64.npz:
+  pos_*      a history with QR > 0 and curvature in log QR (positive_history),
+             its interpolation (QR arrays 1, 3, 5, 7), QKstep/QRstep, and one
+             RK54 step of 1e-3 (pos_rk54_*)
+  ltraj_*    the reference controller run from t=0 with the option on
 """
 from __future__ import annotations
 
@@ -121,6 +128,47 @@ def _indicators(st: O.State, L: int) -> np.ndarray:
     return np.array(vals)
 
 
+def positive_history(theta: np.ndarray, n: int = 60, T: float = 0.6, t_hi: float = 50.0) -> O.State:
+    """QK = (theta t + 1) / (t + 1), QR = 1 / (T (t + 1)) on rows t = 0 and
+    logspace(1e-5, t_hi); row k's derivative columns hold h_k times the
+    derivative at t_{k-1}."""
+    t = np.concatenate([[0.0], np.logspace(-5, np.log10(t_hi), n - 1)])
+    tc = t[:, None]
+    QK = (theta[None, :] * tc + 1.0) / (tc + 1.0)
+    QR = np.broadcast_to(1.0 / (T * (tc + 1.0)), QK.shape).copy()
+    h = np.diff(t, prepend=0.0)[:, None]
+    tp = np.concatenate([[0.0], t[:-1]])[:, None]
+    dQK = h * (theta[None, :] - 1.0) / (tp + 1.0) ** 2
+    dQR = np.broadcast_to(-h / (T * (tp + 1.0) ** 2), QK.shape).copy()
+    dtr = np.zeros(n)
+    dtr[2:] = (t[2:] - t[1:-1]) / (t[1:-1] - t[:-2])
+    return O.State(t, dtr, QK.ravel(), QR.ravel(), dQK.ravel(), dQR.ravel(), np.ones(n), np.zeros(n))
+
+
+def make_log(L: int, Tmax: float, model: O.Model, nsteps: int) -> dict:
+    out = {}
+    g = O.Reference.grid(L, Tmax=Tmax)
+    ref = O.Reference(g, model, threads=1, log_response=True)
+    st = positive_history(g.theta)
+    out.update({k: v for k, v in state_dict("pos", st).items() if v is not None})
+    ref.set_state(st)
+    ref.interpolate()
+    for w in (1, 3, 5, 7):
+        out[f"pos_interp{w}"] = ref.interp(w)
+    out["pos_qk"] = ref.qkstep()
+    out["pos_qr"] = ref.qrstep()
+    ref.set_state(st)
+    ref.interpolate()
+    out["pos_rk54_err"] = np.array([ref.update(1, 1e-3)])
+    out.update(state_dict("pos_rk54", ref.get_state()))
+    ref.init_state()
+    tr = ref.run(nsteps)
+    for k, v in tr.items():
+        out[f"ltraj_{k}"] = v
+    out.update(state_dict("ltraj_final", ref.get_state()))
+    return out
+
+
 def main():
     if not O.Reference.available():
         O.build(reference=True)
@@ -129,6 +177,10 @@ def main():
         path = os.path.join(HERE, f"golden_L{L}.npz")
         np.savez_compressed(path, **data)
         print(path, os.path.getsize(path))
+    L, Tmax, model, nsteps = CASES[1]
+    path = os.path.join(HERE, f"golden_log_L{L}.npz")
+    np.savez_compressed(path, **make_log(L, Tmax, model, nsteps))
+    print(path, os.path.getsize(path))
 
 
 if __name__ == "__main__":
