@@ -65,7 +65,12 @@ class RunParams(C.Structure):
         ("gpu_rollback", C.c_int), ("out_dt", dp), ("out_method", ip), ("out_delta", dp), ("out_t", dp),
         ("out_energy", dp), ("out_qk0", dp), ("out_r", dp),
         ("sparsify_every", C.c_longlong), ("sparsify_sweeps", C.c_int), ("sparsify_variant", C.c_int),
+        ("tail_fit", C.c_int),
     ]
+
+
+class TailInfo(C.Structure):
+    _fields_ = [("alpha_raw", C.c_double), ("alpha", C.c_double), ("j0", C.c_int), ("applied", C.c_int)]
 
 
 class NoAllocRHS(C.Structure):
@@ -141,6 +146,8 @@ def lib():
         sigs = {
             "dyn_abi_version": ([], C.c_int),
             "dyn_energy_history": ([vp, dp, C.c_size_t], C.c_int),
+            "dyn_tail_fit": ([vp, C.c_int, C.POINTER(TailInfo)], C.c_int),
+            "dyn_tail_fit_reset": ([vp], C.c_int),
             "dyn_last_error": ([], C.c_char_p),
             "dyn_ctx_create": ([C.POINTER(Config), C.POINTER(Tables), C.POINTER(vp)], C.c_int),
             "dyn_ctx_destroy": ([vp], C.c_int),

@@ -21,7 +21,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdynamite_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_SOURCES = ["dyn_kernels.cu", "dyn_api.cu", "dyn_mixed.cu", "dyn_batch.cu", "dyn_adjoint.cu", "dyn_noalloc.cu"]
+CU_SOURCES = ["dyn_kernels.cu", "dyn_api.cu", "dyn_mixed.cu", "dyn_batch.cu", "dyn_adjoint.cu", "dyn_noalloc.cu",
+              "dyn_tail.cu"]
 CXX_SOURCES = ["dyn_grid.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

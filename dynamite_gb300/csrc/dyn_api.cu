@@ -60,6 +60,7 @@ struct Ctx {
     size_t n = 0, cap = 0;
     dyn_controller ctl{};
     int last_rollback_loop = -1000;  // loop of the last rollback (simulation_runner.cpp:53, :290)
+    TailState* tail = nullptr;       // tail fit state across calls (device)
     double specRad = 0.0;
     // pinned staging
     StageDev* stages_h = nullptr;
@@ -114,10 +115,11 @@ struct Ctx {
                         d.geS, d.gfS, d.part, d.rowval, d.epart, d.slots, d.stages, d.rhs_out, d.ip,
                         d.rint, scratch_dev, (void*)d.wA1f, (void*)d.wA2f, (void*)d.wB2f, d.KRf, d.dKRf,
                         (void*)d.integ_f, d.inv_len_f, d.inv_dtr_f, d.KRl, (void*)d.wA1l, (void*)d.wA2l,
-                        (void*)d.wB2l};
+                        (void*)d.wB2l, tail};
         for (void* b : bufs) if (b) cudaFree(b);
         std::memset(&d, 0, sizeof d);
         scratch_dev = nullptr;
+        tail = nullptr;
         if (stages_h) cudaFreeHost(stages_h);
         if (slots_h) cudaFreeHost(slots_h);
         if (rhs_h) cudaFreeHost(rhs_h);
@@ -647,6 +649,31 @@ bool sparsify_indices(const unsigned char* fl, size_t n, int variant, const std:
     }
     return true;
 }
+// The tail fit's state starts as the reference's statics do (tail_fit.cpp:81-85)
+static dyn_status tail_reset(Ctx* c) {
+    if (!c->tail && dalloc(&c->tail, 1)) return DYN_ERR_NOMEM;
+    TailState t{};
+    t.prev_off = -1;
+    t.prev_n = 0;
+    t.alpha = 0.0;
+    t.last_rb = -1000;
+    cudaError_t e = cudaMemcpyAsync(c->tail, &t, sizeof t, cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) return fail(DYN_ERR_CUDA, cudaGetErrorString(e));
+    return DYN_OK;
+}
+
+static dyn_status tail_fit(Ctx* c, int rollback_loop) {
+    if (c->d.mixed) return fail(DYN_ERR_UNSUPPORTED, "the tail fit runs on FP64 contexts");
+    if (c->n == 0) return fail(DYN_ERR_STATE, "no state: call dyn_state_init or dyn_state_upload");
+    dyn_status s;
+    if (!c->tail && (s = tail_reset(c))) return s;
+    const cudaError_t e = launch_tail_fit(c->d, (int)c->n, rollback_loop, c->cfg.delta_max, c->tail, c->st);
+    if (e != cudaSuccess) return fail(DYN_ERR_CUDA, cudaGetErrorString(e));
+    c->gen++;  // the newest row may have changed
+    return DYN_OK;
+}
+
 }  // namespace dyn
 
 extern "C" {
@@ -1002,6 +1029,26 @@ dyn_status dyn_energy(void* p, double* e) {
     return DYN_OK;
 }
 
+dyn_status dyn_tail_fit(void* p, int last_rollback_loop, dyn_tail_info* info) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    Ctx* c = C(p);
+    dyn_status s = tail_fit(c, last_rollback_loop);
+    if (s || !info) return s;
+    TailState t;
+    CK(cudaMemcpyAsync(&t, c->tail, sizeof t, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    info->alpha_raw = t.alpha_raw;
+    info->alpha = t.alpha;
+    info->j0 = t.j0;
+    info->applied = t.applied;
+    return DYN_OK;
+}
+
+dyn_status dyn_tail_fit_reset(void* p) {
+    if (!p) return fail(DYN_ERR_INVALID, "null ctx");
+    return tail_reset(C(p));
+}
+
 dyn_status dyn_energy_history(void* p, double* e, size_t n_rows) {
     if (!p || !e) return fail(DYN_ERR_INVALID, "null argument");
     Ctx* c = C(p);
@@ -1060,6 +1107,10 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
         dyn_status s = c->step(k.method, k.delta_t, &r);
         if (s) return s;
         k.delta = r.delta;
+        if (rp->tail_fit) {  // simulation_runner.cpp:135-141
+            if ((s = tail_fit(c, c->last_rollback_loop))) return s;
+            if (rp->out_energy && (s = dyn_energy(p, &r.energy))) return s;  // of the fitted row
+        }
         k.loop++;
         if (rp->sparsify_every > 0 && k.loop % rp->sparsify_every == 0) {
             // simulation_runner.cpp:148-237: sweeps while the history shrinks, then
@@ -1217,6 +1268,7 @@ dyn_status dyn_adjoint_forward(void* p, const dyn_run_params* rp, dyn_step_resul
     if (c->d.logr) return fail(DYN_ERR_UNSUPPORTED, "the adjoint differentiates the linear-domain gathers only");
     if (rp->gpu_rollback || rp->sparsify_every > 0)
         return fail(DYN_ERR_INVALID, "the adjoint needs an append-only history: no rollback, no sparsify");
+    if (rp->tail_fit) return fail(DYN_ERR_UNSUPPORTED, "the adjoint has no tail fit");
     if (c->n == 0) return fail(DYN_ERR_STATE, "no state: call dyn_state_init or dyn_state_upload");
     if (rp->nsteps < 0) return fail(DYN_ERR_INVALID, "nsteps must be non-negative");
     const size_t N = (size_t)rp->nsteps;

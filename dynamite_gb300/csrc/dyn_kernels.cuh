@@ -190,6 +190,21 @@ inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
     return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
+// Window / smoothing state of the tail fit across calls (the reference keeps it
+// in function statics, tail_fit.cpp:81-85); dyn_tail.cu
+struct TailState {
+    long long prev_off;   // offset of the last chosen window (-1: none yet)
+    long long prev_n;     // history rows at the last call
+    double alpha;         // smoothed alpha
+    int last_rb;          // rollback loop seen last (-1000 initially)
+    int applied;          // last call: 1 if QK was blended
+    double alpha_raw;     // last call: the chosen window's mean
+    int j0;               // last call: first blended column
+    int pad;
+};
+cudaError_t launch_tail_fit(const DevCtx& c, int nrows, int rollback_loop, double delta_max, TailState* ts,
+                            cudaStream_t st);
+
 // launch wrappers (dyn_kernels.cu)
 cudaError_t launch_stage(const DevCtx& c, int s, cudaStream_t st);
 cudaError_t launch_main_only(const DevCtx& c, int s, cudaStream_t st);

@@ -202,6 +202,16 @@ class Simulation:
         _lib.check(_lib.lib().dyn_energy_history(self._h, _lib.ptr(out), out.size), "dyn_energy_history")
         return out
 
+    def tail_fit(self, last_rollback_loop: int = -1000) -> dict:
+        """One QK tail fit of the newest row (tailFitBlendCPU, tail_fit.cpp:46-262);
+        the window and the smoothed alpha carry over between calls."""
+        info = _lib.TailInfo()
+        _lib.check(_lib.lib().dyn_tail_fit(self._h, last_rollback_loop, C.byref(info)), "dyn_tail_fit")
+        return dict(alpha_raw=info.alpha_raw, alpha=info.alpha, j0=info.j0, applied=bool(info.applied))
+
+    def tail_fit_reset(self) -> None:
+        _lib.check(_lib.lib().dyn_tail_fit_reset(self._h), "dyn_tail_fit_reset")
+
     def update(self, method: int | None = None, delta_t: float | None = None) -> StepResult:
         c = self.controller
         m = c["method"] if method is None else method
@@ -220,10 +230,12 @@ class Simulation:
         return self.update(serk2_method(q), delta_t)
 
     def run(self, nsteps: int, schedule=None, tmax: float = 0.0, gpu_rollback: bool = False,
-            sparsify_every: int = 0, sparsify_sweeps: int = 1, sparsify_variant: str = "gpu") -> dict:
+            sparsify_every: int = 0, sparsify_sweeps: int = 1, sparsify_variant: str = "gpu",
+            tail_fit: bool = False) -> dict:
         """The driver loop (simulation_runner.cpp:125-304): `nsteps` controller iterations
         (or until t >= tmax); with `sparsify_every` > 0 the periodic sparsify of the
-        reference (every that many loops; the reference uses 100000)."""
+        reference (every that many loops; the reference uses 100000); with `tail_fit`
+        the QK tail fit after every step (the reference's --tail-fit)."""
         out = {k: np.zeros(nsteps) for k in ("dt", "delta", "t", "energy", "qk0", "r")}
         meth = np.zeros(nsteps, dtype=np.int32)
         sd = sm = None
@@ -234,7 +246,7 @@ class Simulation:
                             int(gpu_rollback), _lib.ptr(out["dt"]), meth.ctypes.data_as(_lib.ip),
                             _lib.ptr(out["delta"]), _lib.ptr(out["t"]), _lib.ptr(out["energy"]),
                             _lib.ptr(out["qk0"]), _lib.ptr(out["r"]), sparsify_every, sparsify_sweeps,
-                            SPARSIFY[sparsify_variant])
+                            SPARSIFY[sparsify_variant], int(tail_fit))
         last = _lib.StepResult()
         _lib.check(_lib.lib().dyn_run(self._h, C.byref(rp), C.byref(last)), "dyn_run")
         out["method"] = meth

@@ -162,6 +162,11 @@ typedef struct {
     long long sparsify_every;
     int sparsify_sweeps;
     int sparsify_variant;
+    /* 1: the QK tail fit of the newest row after every step (the reference's
+     * --tail-fit, tail_fit.cpp:46-262, applied at simulation_runner.cpp:135-141);
+     * out_energy is then the energy of the fitted row, as the reference records it.
+     * DYN_FP64 contexts only. */
+    int tail_fit;
 } dyn_run_params;
 
 /* ---------------------------------------------------------------- basics */
@@ -204,6 +209,20 @@ dyn_status dyn_energy(void* ctx, double* e);
  * (computeEnergyHistoryKernel, io_output.cu:61-122), into host e[n_rows]:
  * E_k = -t_k (sum_j w_j f'(QK[k,j]) QR[k,j] + f'(QK[k,0]) / T0). */
 dyn_status dyn_energy_history(void* ctx, double* e, size_t n_rows);
+/* tailFitBlendCPU / tailFitBlendGPU (tail_fit.cpp:46-262, tail_fit.cu): one QK
+ * tail fit of the newest history row, in place.  last_rollback_loop is the loop
+ * of the caller's last rollback (-1000: none; a change resets the smoothing).
+ * The fit keeps its window and smoothed alpha across calls on the context, as
+ * the reference keeps them across a process; dyn_tail_fit_reset forgets them.
+ * info (may be NULL; non-NULL synchronizes) receives this call's raw and
+ * smoothed alpha, first blended column and whether QK was blended.
+ * DYN_FP64 contexts only. */
+typedef struct {
+    double alpha_raw, alpha;
+    int j0, applied;
+} dyn_tail_info;
+dyn_status dyn_tail_fit(void* ctx, int last_rollback_loop, dyn_tail_info* info);
+dyn_status dyn_tail_fit_reset(void* ctx);
 /* ConvAGPU / ConvRGPU (convolution.cu:64-230): kind 0 = A, 1 = R; f, g,
  * out are device arrays, n = len (1-D) or len*len (2-D). */
 dyn_status dyn_conv_dev(void* ctx, int kind, const double* f, const double* g, size_t n, double t,

@@ -25,6 +25,7 @@
 #include "EOMs/time_steps.hpp"
 #include "EOMs/runge_kutta.hpp"
 #include "sparsify/sparsify_utils.hpp"
+#include "simulation/tail_fit.hpp"
 #include "convolution/convolution.hpp"
 #include "math/math_sigma.hpp"
 #include "math/math_ops.hpp"
@@ -35,6 +36,7 @@
 #include "grid/interpolation_weights.hpp"
 
 SimulationConfig config;
+int last_rollback_loop = -1000;  // simulation_runner.cpp:53 (read by the tail fit)
 SimulationData* sim = nullptr;
 RKData* rk = nullptr;
 
@@ -58,6 +60,14 @@ extern "C" {
 // The -R option (config.cpp:164-166): QR gathered in log space by
 // indexVecLN3 / indexVecN / indexMatAll.  dynref_setup resets it to off.
 void dynref_set_log_response(int on) { config.log_response_interp = on != 0; }
+
+// --tail-fit (config.hpp:55): dynref_run applies tailFitBlendCPU after each
+// update; dynref_tail_fit applies it once to the current state.  The fit keeps
+// its window / smoothing state in function statics (tail_fit.cpp:81-85), so a
+// process sees one fit history: drive it from a fresh process.
+void dynref_set_tail_fit(int on) { config.tail_fit_enabled = on != 0; }
+void dynref_tail_fit(void) { tailFitBlendCPU(); }
+void dynref_set_rollback_loop(int loop) { last_rollback_loop = loop; }
 
 // Model / controller parameters (config.hpp:18-56).
 int dynref_setup(int p, int p2, double lambda, double T0, double Gamma, size_t len,
@@ -266,11 +276,13 @@ void dynref_sparsify(double threshold) { sparsifyNscale(threshold); }
 // sparsifyNscale pass at delta_max, interpolate(), then the halving with
 // rk->init = 2 when delta < delta_max/2; no rollback on the CPU, so the last
 // rollback loop stays at its initial -1000, :53).
+// With dynref_set_tail_fit(1), tailFitBlendCPU after every update, as the CUDA
+// build's loop does when --tail-fit is on (:135-141; the CPU-only build's loop
+// has no tail fit).
 int dynref_run(int nsteps, const double* schedule_dt, const int* schedule_method,
                double* out_dt, int* out_method, double* out_delta, double* out_t,
                double* out_energy, long long sparsify_every) {
     const size_t L = config.len;
-    const int last_rollback_loop = -1000;
     for (int k = 0; k < nsteps; ++k) {
         if (schedule_dt) {
             config.delta_t = schedule_dt[k];
@@ -281,6 +293,7 @@ int dynref_run(int nsteps, const double* schedule_dt, const int* schedule_method
         if (out_method) out_method[k] = rk->init;
         config.delta_old = config.delta;
         config.delta = update();
+        if (config.tail_fit_enabled) tailFitBlendCPU();
         config.loop++;
         if (sparsify_every > 0 && config.loop % sparsify_every == 0) {
             sparsifyNscale(config.delta_max);

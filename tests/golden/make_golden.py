@@ -25,6 +25,16 @@ on the grid and model of golden_L64.npz:
              its interpolation (QR arrays 1, 3, 5, 7), QKstep/QRstep, and one
              RK54 step of 1e-3 (pos_rk54_*)
   ltraj_*    the reference controller run from t=0 with the option on
+
+golden_tail_L64.npz: the QK tail fit (--tail-fit, tailFitBlendCPU) on the grid
+and model of golden_L64.npz, in one process (the fit keeps its state in statics):
+  tft_*      the reference controller run from t=0 with the fit after every
+             update (400 steps): per-step records, final t1grid/rvec, the last
+             row, and per-row sums of QK and QR
+  tfs_*      then single fits: state A (the mid state of golden_L64.npz with its
+             newest row's tail replaced by tail_row(theta)) fitted twice; state B
+             (A plus one row, tfB_*) fitted, then with the rollback loop set to 5,
+             then back to -1000; the newest QK row after each fit
 """
 from __future__ import annotations
 
@@ -169,6 +179,66 @@ def make_log(L: int, Tmax: float, model: O.Model, nsteps: int) -> dict:
     return out
 
 
+TAIL_ALPHA = 3.0
+
+
+def tail_row(theta: np.ndarray, qk: np.ndarray) -> np.ndarray:
+    """The newest row with its second half replaced by 1 - a (1 - theta)^2 (1 + 1e-5 sin 7 theta)."""
+    out = qk.copy()
+    h = theta.size // 2
+    th = theta[h:]
+    out[h:] = 1.0 - TAIL_ALPHA * (1.0 - th) ** 2 * (1.0 + 1e-5 * np.sin(7.0 * th))
+    return out
+
+
+def tail_states(mid: O.State, theta: np.ndarray) -> tuple:
+    """State A (mid with tail_row in its newest row) and B (A plus one row)."""
+    L = theta.size
+    QK = mid.QK.copy()
+    QK[-L:] = tail_row(theta, QK[-L:])
+    a = O.State(mid.t1grid.copy(), mid.dtr.copy(), QK, mid.QR.copy(), mid.dQK.copy(), mid.dQR.copy(),
+                mid.rvec.copy(), mid.drvec.copy())
+    t = mid.t1grid
+    tn = t[-1] + 0.5 * (t[-1] - t[-2])
+    rowK = 0.999 * QK[-L:] + 0.001
+    b = O.State(np.append(t, tn), np.append(mid.dtr, 0.5), np.concatenate([QK, rowK]),
+                np.concatenate([mid.QR, mid.QR[-L:]]), np.concatenate([mid.dQK, mid.dQK[-L:]]),
+                np.concatenate([mid.dQR, mid.dQR[-L:]]), np.append(mid.rvec, mid.rvec[-1]),
+                np.append(mid.drvec, mid.drvec[-1]))
+    return a, b
+
+
+def make_tail(L: int, Tmax: float, model: O.Model, mid: O.State, nsteps: int = 400) -> dict:
+    out = {}
+    g = O.Reference.grid(L, Tmax=Tmax)
+    ref = O.Reference(g, model, threads=1)
+    ref.set_tail_fit(True)
+    ref.init_state()
+    tr = ref.run(nsteps)
+    for k, v in tr.items():
+        out[f"tft_{k}"] = v
+    st = ref.get_state()
+    out["tft_t1grid"] = st.t1grid
+    out["tft_rvec"] = st.rvec
+    out["tft_QK_last"] = st.QK[-L:]
+    out["tft_QR_last"] = st.QR[-L:]
+    out["tft_rowsum_QK"] = st.QK.reshape(-1, L).sum(axis=1)
+    out["tft_rowsum_QR"] = st.QR.reshape(-1, L).sum(axis=1)
+    a, b = tail_states(mid, g.theta)
+    rows = []
+    ref.set_state(a)
+    for _ in range(2):
+        ref.tail_fit()
+        rows.append(ref.get_state().QK[-L:])
+    ref.set_state(b)
+    for rb in (-1000, 5, -1000):
+        O.Reference.lib().dynref_set_rollback_loop(rb)
+        ref.tail_fit()
+        rows.append(ref.get_state().QK[-L:])
+    out["tfs_QK"] = np.array(rows)
+    return out
+
+
 def main():
     if not O.Reference.available():
         O.build(reference=True)
@@ -180,6 +250,11 @@ def main():
     L, Tmax, model, nsteps = CASES[1]
     path = os.path.join(HERE, f"golden_log_L{L}.npz")
     np.savez_compressed(path, **make_log(L, Tmax, model, nsteps))
+    print(path, os.path.getsize(path))
+    with np.load(os.path.join(HERE, f"golden_L{L}.npz")) as f:
+        mid = O.State(*(f[f"mid_{k}"] for k in ("t1grid", "dtr", "QK", "QR", "dQK", "dQR", "rvec", "drvec")))
+    path = os.path.join(HERE, f"golden_tail_L{L}.npz")
+    np.savez_compressed(path, **make_tail(L, Tmax, model, mid))
     print(path, os.path.getsize(path))
 
 
