@@ -155,6 +155,7 @@ def lib():
             "dyn_state_init": ([vp, C.c_double], C.c_int),
             "dyn_state_upload": ([vp, C.POINTER(StateC)], C.c_int),
             "dyn_state_rows": ([vp, szp], C.c_int),
+            "dyn_state_time": ([vp, dp], C.c_int),
             "dyn_state_download": ([vp, C.POINTER(StateC)], C.c_int),
             "dyn_controller_get": ([vp, C.POINTER(Controller)], C.c_int),
             "dyn_controller_set": ([vp, C.POINTER(Controller)], C.c_int),

@@ -1,6 +1,7 @@
 """RG-Evo's binary checkpoint `data.bin` (io_save_binary.cpp:66-99, read back by
 io_input.cpp:112-175), so states move between the reference and this library:
-resume a reference run here, or hand one of ours back to RG-Evo.
+resume a reference run here, or hand one of ours back to RG-Evo.  Also the
+"compressed" outputs a save writes beside it (io_save_compressed.cpp:17-63).
 
 Layout (native byte order, as the reference writes it with `ofstream::write`):
 
@@ -18,6 +19,7 @@ does (io_input.cpp:169-172): entries 0 and 1 are 0, entry i >= 2 is
 """
 from __future__ import annotations
 
+import os
 import struct
 from dataclasses import dataclass
 
@@ -84,3 +86,35 @@ def load(path: str) -> tuple[State, CheckpointParams]:
     st = State(arrays["t1grid"], delta_t_ratio(arrays["t1grid"]), arrays["QK"], arrays["QR"], arrays["dQK"],
                arrays["dQR"], arrays["rvec"], arrays["drvec"])
     return st, CheckpointParams(p, p2, lam, T0, Gamma, delta, delta_t, loop, energy)
+
+
+def save_compressed(dir_path: str, QKB1: np.ndarray, QRB1: np.ndarray, theta: np.ndarray, t_last: float) -> None:
+    """QK_compressed / QR_compressed (uint64 rows, uint64 cols, then the L x L B1
+    interpolation, row i = theta_i t) and t1_compressed.txt (t theta_i, fixed with
+    16 decimals), as io_save_compressed.cpp:17-63 writes them."""
+    L = int(np.asarray(theta).size)
+    for name, a in (("QK_compressed", QKB1), ("QR_compressed", QRB1)):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.size != L * L:
+            raise ValueError(f"{name}: {a.size} values, the layout needs {L * L}")
+        with open(os.path.join(dir_path, name), "wb") as fh:
+            fh.write(struct.pack("=QQ", L, L))
+            fh.write(a.tobytes())
+    with open(os.path.join(dir_path, "t1_compressed.txt"), "w") as fh:
+        fh.writelines(f"{t_last * th:.16f}\n" for th in np.asarray(theta, dtype=np.float64))
+
+
+def load_compressed(dir_path: str) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """(QKB1, QRB1, t theta) from the three compressed files."""
+    out = []
+    for name in ("QK_compressed", "QR_compressed"):
+        with open(os.path.join(dir_path, name), "rb") as fh:
+            raw = fh.read()
+        if len(raw) < 16:
+            raise ValueError(f"{name}: truncated header")
+        rows, cols = struct.unpack_from("=QQ", raw, 0)
+        if len(raw) != 16 + 8 * rows * cols:
+            raise ValueError(f"{name}: {len(raw)} bytes, the header promises {16 + 8 * rows * cols}")
+        out.append(np.frombuffer(raw, dtype=np.float64, offset=16).reshape(rows, cols).copy())
+    t = np.loadtxt(os.path.join(dir_path, "t1_compressed.txt"), dtype=np.float64, ndmin=1)
+    return out[0], out[1], t

@@ -881,6 +881,13 @@ dyn_status dyn_state_rows(void* p, size_t* n) {
     return DYN_OK;
 }
 
+dyn_status dyn_state_time(void* p, double* t) {
+    if (!p || !t) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    *t = c->n ? c->t1[c->n - 1] : 0.0;
+    return DYN_OK;
+}
+
 dyn_status dyn_state_download(void* p, dyn_state* stt) {
     if (!p || !stt) return fail(DYN_ERR_INVALID, "null argument");
     Ctx* c = C(p);

@@ -202,6 +202,21 @@ class Simulation:
         _lib.check(_lib.lib().dyn_energy_history(self._h, _lib.ptr(out), out.size), "dyn_energy_history")
         return out
 
+    def save_compressed(self, dir_path: str) -> None:
+        """The compressed outputs of a save (io_save_compressed.cpp:17-63): the B1
+        interpolation QKB1/QRB1 of the current state (reference-order gathers at
+        fresh positions, as the reference holds them after a step) and t theta."""
+        from .checkpoint import save_compressed
+        self.interpolate()
+        save_compressed(dir_path, self.interp(4), self.interp(5), self.grid.theta, self.t)
+
+    @property
+    def t(self) -> float:
+        """The current time (t1grid of the newest row)."""
+        v = C.c_double()
+        _lib.check(_lib.lib().dyn_state_time(self._h, C.byref(v)), "dyn_state_time")
+        return v.value
+
     def tail_fit(self, last_rollback_loop: int = -1000) -> dict:
         """One QK tail fit of the newest row (tailFitBlendCPU, tail_fit.cpp:46-262);
         the window and the smoothed alpha carry over between calls."""

@@ -184,6 +184,8 @@ dyn_status dyn_state_init(void* ctx, double delta_t);
 /* Load / read back the history (loadSimulationState / copyVectorsToCPU). */
 dyn_status dyn_state_upload(void* ctx, const dyn_state* st);
 dyn_status dyn_state_rows(void* ctx, size_t* n);
+/* t1grid of the newest row (the current time); 0 before any state */
+dyn_status dyn_state_time(void* ctx, double* t);
 dyn_status dyn_state_download(void* ctx, dyn_state* st);
 dyn_status dyn_controller_get(void* ctx, dyn_controller* c);
 dyn_status dyn_controller_set(void* ctx, const dyn_controller* c);

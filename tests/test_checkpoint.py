@@ -71,3 +71,27 @@ def test_damaged_files_rejected(tmp_path):
     bad = State(st.t1grid, st.dtr, st.QK[:-1], st.QR, st.dQK, st.dQR, st.rvec, st.drvec)
     with pytest.raises(ValueError):
         ck.save(str(tmp_path / "x.bin"), bad, _params())
+
+
+def test_compressed_outputs_layout_and_round_trip(tmp_path):
+    """io_save_compressed.cpp:17-63: uint64 rows and cols, then L*L doubles of the B1
+    interpolation; t1_compressed.txt holds t theta_i with 16 fixed decimals."""
+    L = 8
+    rng = np.random.default_rng(3)
+    qk, qr = rng.standard_normal(L * L), rng.standard_normal(L * L)
+    theta = np.linspace(0.0, 1.0, L)
+    ck.save_compressed(str(tmp_path), qk, qr, theta, 12.5)
+    raw = (tmp_path / "QK_compressed").read_bytes()
+    assert struct.unpack_from("=QQ", raw, 0) == (L, L) and len(raw) == 16 + 8 * L * L
+    np.testing.assert_array_equal(np.frombuffer(raw, dtype=np.float64, offset=16), qk)
+    lines = (tmp_path / "t1_compressed.txt").read_text().splitlines()
+    assert lines[0] == "0.0000000000000000" and lines[-1] == "12.5000000000000000"
+    a, b, t = ck.load_compressed(str(tmp_path))
+    np.testing.assert_array_equal(a.ravel(), qk)
+    np.testing.assert_array_equal(b.ravel(), qr)
+    np.testing.assert_array_equal(t, 12.5 * theta)
+    with pytest.raises(ValueError):
+        ck.save_compressed(str(tmp_path), qk[:-1], qr, theta, 1.0)
+    (tmp_path / "QK_compressed").write_bytes(raw[:-8])
+    with pytest.raises(ValueError):
+        ck.load_compressed(str(tmp_path))

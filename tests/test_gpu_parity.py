@@ -343,6 +343,22 @@ def test_checkpoint_resume_continues_bit_for_bit(product_built, tmp_path):
         np.testing.assert_array_equal(getattr(sa, k), getattr(sb, k), err_msg=k)
 
 
+@pytest.mark.parametrize("L", SIZES)
+def test_compressed_outputs_hold_the_reference_b1_interpolation(product_built, L, tmp_path):
+    """A save's QK_compressed / QR_compressed of the mid state: the reference's own
+    B1 arrays at fresh positions, bit for bit."""
+    from dynamite_gb300 import checkpoint as ck
+    g = load_golden(L)
+    s = sim_for(g)
+    s.upload(state_from(g, "mid", D.State))
+    s.save_compressed(str(tmp_path))
+    qk, qr, t = ck.load_compressed(str(tmp_path))
+    np.testing.assert_array_equal(qk.ravel(), g["mid_interp4"])
+    np.testing.assert_array_equal(qr.ravel(), g["mid_interp5"])
+    np.testing.assert_array_equal(t, np.array([float(f"{x:.16f}") for x in g["mid_t1grid"][-1] * g["grid_theta"]]))
+    assert s.t == g["mid_t1grid"][-1]
+
+
 def test_energy_history_as_the_reference_saves_it(product_built):
     """computeEnergyHistoryKernel (io_output.cu:61-122) restated in numpy: E_k = -t_k (sum_j
     w_j f'(QK[k,j]) QR[k,j] + f'(QK[k,0]) / T0) over every row of a mid-run history."""
