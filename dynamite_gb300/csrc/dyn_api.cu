@@ -663,12 +663,16 @@ static dyn_status tail_reset(Ctx* c) {
     return DYN_OK;
 }
 
+// The fit edits the FP64 master row; the mixed forms' FP32 mirrors of that row follow.
 static dyn_status tail_fit(Ctx* c, int rollback_loop) {
-    if (c->d.mixed) return fail(DYN_ERR_UNSUPPORTED, "the tail fit runs on FP64 contexts");
     if (c->n == 0) return fail(DYN_ERR_STATE, "no state: call dyn_state_init or dyn_state_upload");
     dyn_status s;
     if (!c->tail && (s = tail_reset(c))) return s;
-    const cudaError_t e = launch_tail_fit(c->d, (int)c->n, rollback_loop, c->cfg.delta_max, c->tail, c->st);
+    DevCtx& d = c->d;
+    const size_t row = (c->n - 1) * (size_t)c->L;
+    cudaError_t e = launch_tail_fit(d, (int)c->n, rollback_loop, c->cfg.delta_max, c->tail, c->st);
+    if (e == cudaSuccess && d.mixed) e = launch_mirror_rows(d.KR + row, d.KRf + row, c->L, c->st);
+    if (e == cudaSuccess && d.KRl) e = launch_mirror_lo(d.KR + row, d.KRl + row, c->L, c->st);
     if (e != cudaSuccess) return fail(DYN_ERR_CUDA, cudaGetErrorString(e));
     c->gen++;  // the newest row may have changed
     return DYN_OK;

@@ -164,8 +164,7 @@ typedef struct {
     int sparsify_variant;
     /* 1: the QK tail fit of the newest row after every step (the reference's
      * --tail-fit, tail_fit.cpp:46-262, applied at simulation_runner.cpp:135-141);
-     * out_energy is then the energy of the fitted row, as the reference records it.
-     * DYN_FP64 contexts only. */
+     * out_energy is then the energy of the fitted row, as the reference records it. */
     int tail_fit;
 } dyn_run_params;
 
@@ -217,8 +216,8 @@ dyn_status dyn_energy_history(void* ctx, double* e, size_t n_rows);
  * The fit keeps its window and smoothed alpha across calls on the context, as
  * the reference keeps them across a process; dyn_tail_fit_reset forgets them.
  * info (may be NULL; non-NULL synchronizes) receives this call's raw and
- * smoothed alpha, first blended column and whether QK was blended.
- * DYN_FP64 contexts only. */
+ * smoothed alpha, first blended column and whether QK was blended.  On the
+ * mixed forms the fit edits the FP64 row and refreshes its FP32 mirror. */
 typedef struct {
     double alpha_raw, alpha;
     int j0, applied;

@@ -170,11 +170,27 @@ def test_gpu_tail_fit_equals_oracle_bit_for_bit(product_built):
 
 
 @pytest.mark.gpu
-def test_gpu_tail_fit_fp64_only(product_built):
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_gpu_tail_fit_on_the_mixed_forms(product_built, precision):
+    """The fit edits the FP64 row and refreshes the FP32 mirror: a mixed run with
+    the fit stays within the mixed form's tolerance of the FP64 run with the fit,
+    on the same schedule, and the single fits equal the FP64 context's."""
     import dynamite_gb300 as D
-    from dynamite_gb300 import _lib
-    g = load_golden(32)
-    s = D.Simulation(grid_from(g, D.Grid), model_from(g, D.Model), precision="mixed")
-    s.init()
-    with pytest.raises(_lib.DynError, match="FP64"):
+    g, tg = load_golden(64), load_tail_golden()
+    L = 64
+    sched = (tg["tft_dt"], tg["tft_method"])
+    runs = {}
+    for prec in ("fp64", precision):
+        s = D.Simulation(grid_from(g, D.Grid), model_from(g, D.Model), precision=prec)
+        s.init()
+        tr = s.run(tg["tft_dt"].size, schedule=sched, tail_fit=True)
+        runs[prec] = (s, tr)
+    a, b = runs["fp64"][0].download(), runs[precision][0].download()
+    assert rel_err(b.QK, a.QK) < 1e-6 and rel_err(b.QR, a.QR) < 1e-6
+    assert rel_err(runs[precision][1]["energy"], runs["fp64"][1]["energy"]) < 1e-6
+    sa, _ = _states(g, D.State)
+    for s in (runs["fp64"][0], runs[precision][0]):
+        s.tail_fit_reset()
+        s.upload(sa)
         s.tail_fit()
+    np.testing.assert_array_equal(runs[precision][0].download().QK[-L:], runs["fp64"][0].download().QK[-L:])
