@@ -65,7 +65,7 @@ class RunParams(C.Structure):
         ("gpu_rollback", C.c_int), ("out_dt", dp), ("out_method", ip), ("out_delta", dp), ("out_t", dp),
         ("out_energy", dp), ("out_qk0", dp), ("out_r", dp),
         ("sparsify_every", C.c_longlong), ("sparsify_sweeps", C.c_int), ("sparsify_variant", C.c_int),
-        ("tail_fit", C.c_int),
+        ("tail_fit", C.c_int), ("use_serk2", C.c_int),
     ]
 
 
@@ -104,7 +104,7 @@ class BatchConfig(C.Structure):
         ("device", C.c_int), ("stream", C.c_void_p), ("search", C.c_int), ("gpu_rollback", C.c_int),
         ("ticks_per_launch", C.c_int), ("threads", C.c_int), ("targets", C.c_int), ("ctas_per_sm", C.c_int),
         ("sparsify_every", C.c_longlong), ("sparsify_sweeps", C.c_int), ("sparsify_variant", C.c_int),
-        ("precision", C.c_int),
+        ("precision", C.c_int), ("use_serk2", C.c_int),
     ]
 
 

@@ -52,7 +52,7 @@ class Batch:
     def __init__(self, grids: list[Grid], quenches: list[Quench], search: str = "binary", gpu_rollback: bool = False,
                  ticks_per_launch: int = 32, threads: int = 128, targets: int = 1, ctas_per_sm: int = 0,
                  device: int = 0, stream: int | None = None, sparsify_every: int = 0, sparsify_sweeps: int = 1,
-                 sparsify_variant: str = "gpu", precision: str = "mixed"):
+                 sparsify_variant: str = "gpu", precision: str = "mixed", use_serk2: bool = False):
         self.grids = grids
         self.quenches = list(quenches)
         self._h = C.c_void_p()
@@ -71,7 +71,7 @@ class Batch:
                                      q.t_stop, q.max_steps, q.capacity)
         cfg = _lib.BatchConfig(device, stream, SEARCH[search], int(gpu_rollback), ticks_per_launch, threads, targets,
                                ctas_per_sm, sparsify_every, sparsify_sweeps, SPARSIFY[sparsify_variant],
-                               {"mixed": 1, "mixed_df": 2}[precision])
+                               {"mixed": 1, "mixed_df": 2}[precision], int(use_serk2))
         _lib.check(_lib.lib().dyn_batch_create(C.byref(cfg), gs, len(grids), qs, len(quenches), C.byref(self._h)),
                    "dyn_batch_create")
         del keep  # the tables were copied to the device

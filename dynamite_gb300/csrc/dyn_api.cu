@@ -1137,6 +1137,7 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
             if (!rp->dt_schedule && k.delta < dmax / 2 && k.loop - c->last_rollback_loop > 1000) {
                 k.delta_t *= 0.5;
                 if (k.method == DYN_RK54) k.method = DYN_SSPRK104;
+                else if (rp->use_serk2 && k.method < 2 + SMAX / 4) k.method++;  // init_SERK2(2 (init - 1))
             }
         }
         if (!rp->dt_schedule) {

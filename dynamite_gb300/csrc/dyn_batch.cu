@@ -604,6 +604,7 @@ struct Batch {
             if (pl.delta < dmax / 2 && pl.loop - pl.last_rb > 1000) {
                 pl.dt *= 0.5;
                 if (pl.method == DYN_RK54) pl.method = DYN_SSPRK104;
+                else if (cfg.use_serk2 && pl.method < 2 + QMAX / 2) pl.method++;  // as dyn_run
             }
             pl.spars_loop = pl.loop;
             pl.status = DYN_QUENCH_RUNNING;

@@ -246,11 +246,12 @@ class Simulation:
 
     def run(self, nsteps: int, schedule=None, tmax: float = 0.0, gpu_rollback: bool = False,
             sparsify_every: int = 0, sparsify_sweeps: int = 1, sparsify_variant: str = "gpu",
-            tail_fit: bool = False) -> dict:
+            tail_fit: bool = False, use_serk2: bool = False) -> dict:
         """The driver loop (simulation_runner.cpp:125-304): `nsteps` controller iterations
         (or until t >= tmax); with `sparsify_every` > 0 the periodic sparsify of the
-        reference (every that many loops; the reference uses 100000); with `tail_fit`
-        the QK tail fit after every step (the reference's --tail-fit)."""
+        reference (every that many loops; the reference uses 100000), whose step halving
+        with `use_serk2` also climbs one SERK2 level; with `tail_fit` the QK tail fit
+        after every step (the reference's --tail-fit)."""
         out = {k: np.zeros(nsteps) for k in ("dt", "delta", "t", "energy", "qk0", "r")}
         meth = np.zeros(nsteps, dtype=np.int32)
         sd = sm = None
@@ -261,7 +262,7 @@ class Simulation:
                             int(gpu_rollback), _lib.ptr(out["dt"]), meth.ctypes.data_as(_lib.ip),
                             _lib.ptr(out["delta"]), _lib.ptr(out["t"]), _lib.ptr(out["energy"]),
                             _lib.ptr(out["qk0"]), _lib.ptr(out["r"]), sparsify_every, sparsify_sweeps,
-                            SPARSIFY[sparsify_variant], int(tail_fit))
+                            SPARSIFY[sparsify_variant], int(tail_fit), int(use_serk2))
         last = _lib.StepResult()
         _lib.check(_lib.lib().dyn_run(self._h, C.byref(rp), C.byref(last)), "dyn_run")
         out["method"] = meth

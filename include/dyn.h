@@ -166,6 +166,12 @@ typedef struct {
      * --tail-fit, tail_fit.cpp:46-262, applied at simulation_runner.cpp:135-141);
      * out_energy is then the energy of the fitted row, as the reference records it. */
     int tail_fit;
+    /* 1: at the periodic block's step halving a method other than RK54 moves one
+     * SERK2 level up (SSPRK(10,4) -> SERK2(2) -> SERK2(4) ...; the GPU loop's
+     * init_SERK2(2 (init - 1)), simulation_runner.cpp:222-229, the reference's
+     * default --serk2 true), at most to SERK2(16); 0: it stays (RK54 still gives
+     * way to SSPRK(10,4)) */
+    int use_serk2;
 } dyn_run_params;
 
 /* ---------------------------------------------------------------- basics */
@@ -334,6 +340,7 @@ typedef struct {
     int sparsify_sweeps;
     int sparsify_variant;
     int precision;           /* DYN_MIXED (or 0) | DYN_MIXED_DF */
+    int use_serk2;           /* the periodic block's SERK2 climb, as dyn_run_params */
 } dyn_batch_config;
 
 /* Quench status */

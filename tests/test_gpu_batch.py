@@ -153,16 +153,18 @@ def test_batch_periodic_sparsify_equals_single(product_built, precision):
     kw2["delta_max"] = 1e-7
     m2 = D.Model(**kw2)
     specs = [(0, m, 70), (1, m2, 45)]
-    for variant in ("gpu", "cpu"):
+    for variant, serk2 in (("gpu", False), ("cpu", False), ("gpu", True)):
         b = D.Batch(grids, [_quench(gi, mm, max_steps=n) for gi, mm, n in specs], ticks_per_launch=16,
-                    sparsify_every=20, sparsify_variant=variant, precision=precision)
+                    sparsify_every=20, sparsify_variant=variant, precision=precision, use_serk2=serk2)
         b.run(100_000)
+        if serk2:
+            assert b.info(0)["method"] >= 3  # climbed past SSPRK(10,4)
         for q, (gi, mm, n) in enumerate(specs):
             inf = b.info(q)
             assert inf["status"] == "max_steps" and inf["steps"] == n
             s = D.Simulation(grids[gi], mm, precision=precision)
             s.init()
-            tr = s.run(n, sparsify_every=20, sparsify_variant=variant)
+            tr = s.run(n, sparsify_every=20, sparsify_variant=variant, use_serk2=serk2)
             st = s.download()
             assert st.t1grid.size < n + 1  # rows were dropped
             _assert_same_state(b.download(q), st)

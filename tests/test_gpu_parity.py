@@ -316,6 +316,32 @@ def test_periodic_sparsify_free_controller(product_built):
         assert (c["delta_t"], c["method"]) == p.controller()
 
 
+def test_periodic_sparsify_serk2_climb(product_built):
+    """use_serk2 (the reference's default on its GPU loop, simulation_runner.cpp:222-229):
+    every periodic halving moves a method past RK54 one SERK2 level up.  The free GPU
+    run makes the oracle's method and step choices, except where an error estimate
+    sits within rounding of a threshold."""
+    g = load_golden(32)
+    p = O.Port(grid_from(g, O.Grid), _spars_model(g, O.Model), search_mode=1, threads=4)
+    p.init_state()
+    tr = p.run(100, sparsify_every=20, sparsify_variant=2, use_serk2=True)
+    assert tr["method"].max() >= 4  # SSPRK(10,4) -> SERK2(2) -> SERK2(4) ...
+    s = D.Simulation(grid_from(g, D.Grid), _spars_model(g, D.Model))
+    s.init()
+    tg = s.run(100, sparsify_every=20, sparsify_variant="gpu", use_serk2=True)
+    same = (tg["dt"] == tr["dt"]) & (tg["method"] == tr["method"])
+    if not same.all():
+        k = int(np.argmin(same))
+        d, dmax = tr["delta"][k - 1], 1e-7
+        near = min(abs(d - dmax), abs(d - 2 * dmax), abs(d - dmax / 2), abs(d - 1.1 * tr["delta"][k - 2])) / dmax
+        assert near < 1e-3, f"schedules diverge at step {k} away from a threshold"
+    else:
+        a, b = s.download(), p.get_state()
+        np.testing.assert_array_equal(a.t1grid, b.t1grid)
+        assert rel_err(a.QK, b.QK) < TRAJ_TOL
+        assert (s.controller["delta_t"], s.controller["method"]) == p.controller()
+
+
 def test_checkpoint_resume_continues_bit_for_bit(product_built, tmp_path):
     """A run saved to RG-Evo's data.bin and loaded into a fresh context continues exactly
     as the original (the loader's delta_t_ratio rebuild leaves the rows the stencils use
