@@ -51,7 +51,7 @@ class Quench:
 class Batch:
     def __init__(self, grids: list[Grid], quenches: list[Quench], search: str = "binary", gpu_rollback: bool = False,
                  ticks_per_launch: int = 32, threads: int = 128, targets: int = 1, ctas_per_sm: int = 0,
-                 device: int = 0, stream: int | None = None, sparsify_every: int = 0, sparsify_sweeps: int = 1,
+                 device: int = 0, stream: int | None = None, sparsify_every: int = 0, sparsify_sweeps: int = -1,
                  sparsify_variant: str = "gpu", precision: str = "mixed", use_serk2: bool = False):
         self.grids = grids
         self.quenches = list(quenches)

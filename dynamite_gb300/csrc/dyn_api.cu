@@ -538,6 +538,14 @@ bool check_tables(size_t L, size_t m, const dyn_tables* tb, std::vector<int> i32
     return true;
 }
 
+int sparsify_block_sweeps(int requested) {
+    if (requested >= 0) return std::min(10, requested);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 1;
+    const double total_mb = (double)(total_b >> 20), used_mb = (double)((total_b - free_b) >> 20);
+    return (total_mb > 0 && used_mb > total_mb * 0.5) ? 2 : 1;
+}
+
 // SERK2 coefficients (runge_kutta.cu:202-272), long double solve
 static long double chebT(int n, long double x) {
     if (n == 0) return 1.0L;
@@ -1127,7 +1135,7 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
             // simulation_runner.cpp:148-237: sweeps while the history shrinks, then
             // (outside a replayed schedule) the step halving
             size_t prev = c->n;
-            const int sweeps = std::min(10, rp->sparsify_sweeps > 0 ? rp->sparsify_sweeps : 1);
+            const int sweeps = sparsify_block_sweeps(rp->sparsify_sweeps);
             for (int sw = 0; sw < sweeps; ++sw) {
                 size_t nn = prev;
                 if ((s = dyn_sparsify(p, dmax, rp->sparsify_variant, &nn))) return s;

@@ -592,7 +592,7 @@ struct Batch {
             any = true;
             Plan& pl = plan_h[b];
             const double dmax = qh[b].dmax;
-            const int sweeps = std::min(10, cfg.sparsify_sweeps > 0 ? cfg.sparsify_sweeps : 1);
+            const int sweeps = sparsify_block_sweeps(cfg.sparsify_sweeps);
             int prev = pl.n;
             for (int sw = 0; sw < sweeps; ++sw) {
                 int nn = prev;

@@ -36,6 +36,11 @@ inline constexpr double SSP_B2[10] = {0., 2.0 / 9, 0, 0, 5.0 / 18, 1.0 / 3, 0., 
 // SERK2(q) combination coefficients b[0..2q] (runge_kutta.cu:202-272), long double solve
 std::vector<double> serk_coeffs(int q);
 
+// Sparsify passes of one periodic block (simulation_runner.cpp:163-183, 187):
+// requested < 0 is the reference's "auto" (2 when more than half of the
+// device's memory is in use, else 1), 0 none, otherwise at most 10
+int sparsify_block_sweeps(int requested);
+
 // pow_int (math_ops.cpp:7-21) on the host
 inline double pow_int_h(double b, int e) {
     if (e == 0) return 1.0;

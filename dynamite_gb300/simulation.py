@@ -245,7 +245,7 @@ class Simulation:
         return self.update(serk2_method(q), delta_t)
 
     def run(self, nsteps: int, schedule=None, tmax: float = 0.0, gpu_rollback: bool = False,
-            sparsify_every: int = 0, sparsify_sweeps: int = 1, sparsify_variant: str = "gpu",
+            sparsify_every: int = 0, sparsify_sweeps: int = -1, sparsify_variant: str = "gpu",
             tail_fit: bool = False, use_serk2: bool = False) -> dict:
         """The driver loop (simulation_runner.cpp:125-304): `nsteps` controller iterations
         (or until t >= tmax); with `sparsify_every` > 0 the periodic sparsify of the

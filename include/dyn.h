@@ -156,9 +156,10 @@ typedef struct {
     /* periodic sparsify of the driver loop (simulation_runner.cpp:148-237): after
      * every loop that is a multiple of sparsify_every (0: never; the reference
      * uses 100000), up to sparsify_sweeps passes of dyn_sparsify(delta_max,
-     * sparsify_variant) while the history shrinks (<= 0: one pass, at most 10),
-     * then, if delta < delta_max/2 and the last rollback is more than 1000
-     * loops back, delta_t halves and RK54 gives way to SSPRK(10,4) */
+     * sparsify_variant) while the history shrinks (at most 10; 0: none; -1: the
+     * reference's default "auto", 2 when more than half of the device's memory is
+     * in use, else 1), then, if delta < delta_max/2 and the last rollback is more
+     * than 1000 loops back, delta_t halves and RK54 gives way to SSPRK(10,4) */
     long long sparsify_every;
     int sparsify_sweeps;
     int sparsify_variant;

@@ -316,6 +316,31 @@ def test_periodic_sparsify_free_controller(product_built):
         assert (c["delta_t"], c["method"]) == p.controller()
 
 
+def test_periodic_block_sweep_counts(product_built):
+    """sparsify_sweeps (simulation_runner.cpp:163-187): 0 runs the block without a
+    pass (no row dropped, the step still halves), -1 ("auto", the reference's
+    default) is one pass on a device less than half full."""
+    g = load_golden(32)
+    p = O.Port(grid_from(g, O.Grid), _spars_model(g, O.Model), search_mode=1, threads=4)
+    p.init_state()
+    tr = p.run(70, sparsify_every=20, sparsify_sweeps=0)
+    assert p.get_state().t1grid.size == 71 and tr["dt"][20] == 0.5 * tr["dt"][19]
+    s = D.Simulation(grid_from(g, D.Grid), _spars_model(g, D.Model))
+    s.init()
+    tg = s.run(70, sparsify_every=20, sparsify_sweeps=0)
+    np.testing.assert_array_equal(tg["dt"], tr["dt"])
+    np.testing.assert_array_equal(s.download().t1grid, p.get_state().t1grid)
+    runs = []
+    for sweeps in (-1, 1):
+        s = D.Simulation(grid_from(g, D.Grid), _spars_model(g, D.Model))
+        s.init()
+        s.run(70, sparsify_every=20, sparsify_sweeps=sweeps)
+        runs.append(s.download())
+    assert runs[0].t1grid.size < 71
+    np.testing.assert_array_equal(runs[0].t1grid, runs[1].t1grid)
+    np.testing.assert_array_equal(runs[0].QK, runs[1].QK)
+
+
 def test_periodic_sparsify_serk2_climb(product_built):
     """use_serk2 (the reference's default on its GPU loop, simulation_runner.cpp:222-229):
     every periodic halving moves a method past RK54 one SERK2 level up.  The free GPU
