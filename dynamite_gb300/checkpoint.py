@@ -1,7 +1,8 @@
 """RG-Evo's binary checkpoint `data.bin` (io_save_binary.cpp:66-99, read back by
 io_input.cpp:112-175), so states move between the reference and this library:
 resume a reference run here, or hand one of ours back to RG-Evo.  Also the
-"compressed" outputs a save writes beside it (io_save_compressed.cpp:17-63).
+"compressed" outputs a save writes beside it (io_save_compressed.cpp:17-63) and
+the per-step log correlation.txt (simulation_runner.cpp:83-91, 326-340).
 
 Layout (native byte order, as the reference writes it with `ofstream::write`):
 
@@ -118,3 +119,14 @@ def load_compressed(dir_path: str) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         out.append(np.frombuffer(raw, dtype=np.float64, offset=16).reshape(rows, cols).copy())
     t = np.loadtxt(os.path.join(dir_path, "t1_compressed.txt"), dtype=np.float64, ndmin=1)
     return out[0], out[1], t
+
+
+def append_correlation(path: str, t, energy, qk0) -> None:
+    """Append `t<TAB>E<TAB>QK(t,0)` lines with 14 fixed decimals to correlation.txt, as the
+    reference's loop logs every step (simulation_runner.cpp:83-91, 326-340); the
+    arrays are `Simulation.run`'s "t", "energy" and "qk0" records."""
+    t, energy, qk0 = (np.atleast_1d(np.asarray(a, dtype=np.float64)) for a in (t, energy, qk0))
+    if not (t.size == energy.size == qk0.size):
+        raise ValueError("t, energy and qk0 must have the same length")
+    with open(path, "a") as fh:
+        fh.writelines(f"{a:.14f}\t{b:.14f}\t{c:.14f}\n" for a, b, c in zip(t, energy, qk0))

@@ -95,3 +95,16 @@ def test_compressed_outputs_layout_and_round_trip(tmp_path):
     (tmp_path / "QK_compressed").write_bytes(raw[:-8])
     with pytest.raises(ValueError):
         ck.load_compressed(str(tmp_path))
+
+
+def test_correlation_log_format(tmp_path):
+    """simulation_runner.cpp:83-91, 326-340: appended lines, std::fixed, 14 decimals."""
+    path = str(tmp_path / "correlation.txt")
+    ck.append_correlation(path, [1e-5, 2.5], [-0.125, -1.0 / 3.0], [1.0, 0.75])
+    ck.append_correlation(path, 3.0, -0.5, 0.5)
+    lines = open(path).read().splitlines()
+    assert lines == ["0.00001000000000\t-0.12500000000000\t1.00000000000000",
+                     "2.50000000000000\t-0.33333333333333\t0.75000000000000",
+                     "3.00000000000000\t-0.50000000000000\t0.50000000000000"]
+    with pytest.raises(ValueError):
+        ck.append_correlation(path, [1.0, 2.0], [1.0], [1.0])
