@@ -464,6 +464,11 @@ struct Batch {
         if (pp == 1) { OCC_SEL(3, 4); } else if (pp == 2) { OCC_SEL(3, 0); } else { OCC_SEL(-1, -1); }
 #undef OCC_SEL
 #undef OCC_T
+        // the (hi, lo) form stages 2 (Lmax + 2) float2: above 48 KB from Lmax = 3071 on; the
+        // attribute is set here, before the tile's first launch and any graph capture
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return 1;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, threads, smem) != cudaSuccess) return 1;
         return nb > 0 ? nb : 1;
     }

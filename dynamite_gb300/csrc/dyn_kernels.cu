@@ -664,12 +664,9 @@ template <int M, int K, int P, int P2, bool LOGR>
 static cudaError_t launch_main_t(const DevCtx& c, int s, cudaStream_t st) {
     dim3 grid(c.nch, c.L), block(c.tpb);
     const size_t smem = (size_t)c.L * (LOGR ? sizeof(double2) + sizeof(double) : sizeof(double2));
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_main<M, K, P, P2, LOGR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             LOGR ? 96 * 1024 : 64 * 1024);
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> devs{0};
+    const cudaError_t e = raise_smem_limit(k_main<M, K, P, P2, LOGR>, smem, 4096 * (int)(smem / c.L), devs);
+    if (e != cudaSuccess) return e;
     return launch_pdl(k_main<M, K, P, P2, LOGR>, grid, block, smem, st, c, s);
 }
 

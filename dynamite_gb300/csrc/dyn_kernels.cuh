@@ -1,5 +1,6 @@
 // Kernel-side structures shared by dyn_kernels.cu and dyn_api.cu.
 #pragma once
+#include <atomic>
 #include <cstddef>
 #include <cuda_runtime.h>
 #include "dyn_common.cuh"
@@ -188,6 +189,22 @@ inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
     cfg.attrs = at;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// Dynamic shared memory above the 48 KB default needs the kernel's
+// MaxDynamicSharedMemorySize attribute, which is per device: raise it to
+// `limit` once per (kernel, device); `devs` is the caller's per-kernel record.
+template <typename Kern>
+inline cudaError_t raise_smem_limit(Kern kern, size_t bytes, int limit, std::atomic<unsigned long long>& devs) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (devs.load() & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+    if (e == cudaSuccess) devs.fetch_or(bit);
+    return e;
 }
 
 // Window / smoothing state of the tail fit across calls (the reference keeps it

@@ -57,7 +57,11 @@ namespace {
 template <int M, int K, int P, int P2>
 cudaError_t launch_df(const DevCtx& c, int s, cudaStream_t st) {
     dim3 grid(c.nch, c.L), block(c.tpb);
-    return launch_pdl(k_main_df<M, K, P, P2>, grid, block, 2 * (size_t)(c.L + 2) * sizeof(float2), st, c, s);
+    const size_t smem = 2 * (size_t)(c.L + 2) * sizeof(float2);  // > 48 KB from L = 3071 on
+    static std::atomic<unsigned long long> devs{0};
+    const cudaError_t e = raise_smem_limit(k_main_df<M, K, P, P2>, smem, 2 * (4096 + 2) * (int)sizeof(float2), devs);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(k_main_df<M, K, P, P2>, grid, block, smem, st, c, s);
 }
 
 template <int M, int K, int P, int P2>

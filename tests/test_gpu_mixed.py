@@ -103,3 +103,24 @@ def test_mixed_df_large_grid_vs_fp64(product_built):
     assert rel_err(tb["energy"], ta["energy"]) < MIXED_DF_TOL
     assert rel_err(sb.QK, sa.QK) < MIXED_DF_TOL
     assert rel_err(sb.QR, sa.QR) < MIXED_DF_TOL
+
+
+def test_df_beyond_the_default_shared_memory(product_built):
+    """The (hi, lo) form stages 2 (L + 2) float2 of the newest row, more than the 48 KB
+    default from L = 3071 on (the kernels raise their limit per device).  At L = 3200 a
+    short run alone and in a batch agrees with the FP64 form and with each other."""
+    L = 3200
+    grid = D.grid.generate(L)
+    m = D.Model(p=3, p2=4, lam=0.5, Gamma=0.6)
+    a = D.Simulation(grid, m, history_capacity=16)
+    a.init()
+    a.run(4)
+    b = D.Simulation(grid, m, precision="mixed_df", history_capacity=16)
+    b.init()
+    b.run(4)
+    qa, qb = a.download().QK, b.download().QK
+    assert rel_err(qb, qa) < 1e-8
+    bt = D.Batch([grid], [D.Quench(max_steps=4, capacity=16)], precision="mixed_df", ticks_per_launch=8)
+    bt.run(1000)
+    np.testing.assert_array_equal(bt.download(0).QK, qb)
+    bt.close()
