@@ -10,8 +10,8 @@
  * order of each floating-point expression is kept as written in the
  * reference so that, compiled with -ffp-contract=off, results are bit-equal
  * to the reference CPU build compiled with the same flags (pinned by
- * tests/test_oracle_vs_reference.py against oracle/_ref and the committed
- * golden vectors).  Outer loops are OpenMP-parallel like the reference;
+ * tests/test_oracle.py, test_log_response.py, test_tail_fit.py and
+ * test_grid_shapes.py against oracle/_ref and the committed golden vectors).  Outer loops are OpenMP-parallel like the reference;
  * every reduction is sequential in index order (the reference's single-
  * thread order), so results do not depend on the thread count.
  *
