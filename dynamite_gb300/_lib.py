@@ -194,6 +194,9 @@ def lib():
             "dyn_adjoint_history_grad": ([vp, C.POINTER(StateC)], C.c_int),
             "dyn_grid_generate": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                    dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
+            "dyn_grid_rational_depth": ([C.c_size_t, C.c_int, C.c_int], C.c_int),
+            "dyn_grid_generate_rational": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                            dp, dp, dp, dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
         }
         for name, (args, res) in sigs.items():
             f = getattr(L, name)

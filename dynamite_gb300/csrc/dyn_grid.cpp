@@ -203,14 +203,16 @@ std::vector<ld> integration_weights(const std::vector<ld>& th, int order) {
 }
 
 // ---- local barycentric stencils (interpolation_weights.cpp:12-147) ----
-int stencil_start(const std::vector<ld>& x, int n, ld xq) {
-    const int N = (int)x.size(), m = n + 1;
+// start of the m-point window around xq whose farther end is nearest
+// (pick_stencil_start with m = n + 1, pick_window_start for any m)
+int window_start(const std::vector<ld>& x, int m, ld xq) {
+    const int N = (int)x.size();
     const int hi = (int)(std::lower_bound(x.begin(), x.end(), xq) - x.begin());
     int start = hi - m / 2;
     if (start < 0) start = 0;
     if (start > N - m) start = N - m;
     auto spread = [&](int s) {
-        const ld l = std::fabs(xq - x[s]), r = std::fabs(xq - x[s + n]);
+        const ld l = std::fabs(xq - x[s]), r = std::fabs(xq - x[s + m - 1]);
         return l < r ? r : l;
     };
     ld best = spread(start);
@@ -227,7 +229,7 @@ void stencils(const std::vector<ld>& x, const std::vector<ld>& xq, int n, int64_
 #pragma omp parallel for schedule(static)
     for (long long k = 0; k < Q; ++k) {
         const ld q = xq[k];
-        const int start = stencil_start(x, n, q);
+        const int start = window_start(x, m, q);
         ld xn[64], wl[64], tmp[64];
         for (int j = 0; j < m; ++j) xn[j] = x[start + j];
         int exact = -1;
@@ -251,6 +253,107 @@ void stencils(const std::vector<ld>& x, const std::vector<ld>& xq, int n, int64_
     }
 }
 
+// ---- Floater-Hormann rational stencils (interpolation_weights.cpp:72-290) ----
+// Barycentric weights of the order-d Floater-Hormann interpolant on the m
+// nodes xn: w_j = sum over the (d+1)-node subsets i..i+d holding j of
+// (-1)^i / prod_{k != j} (x_j - x_k).
+void fh_node_weights(const ld* xn, int m, int d, ld* w) {
+    for (int j = 0; j < m; ++j) {
+        const int r0 = std::max(0, j - (m - d - 1)), r1 = std::min(d, j);
+        ld sum = 0.0L;
+        for (int r = r0; r <= r1; ++r) {
+            const int i = j - r;
+            ld prod = 1.0L;
+            bool dup = false;
+            for (int k = 0; k <= d; ++k) {
+                if (k == r) continue;
+                const ld diff = xn[j] - xn[i + k];
+                if (diff == 0.0L) { dup = true; break; }
+                prod *= diff;
+            }
+            if (dup || prod == 0.0L) continue;
+            sum += (((j - r) & 1) ? -1.0L : 1.0L) / prod;
+        }
+        w[j] = sum;
+    }
+}
+
+// Neumaier-compensated barycentric evaluation at qn: alpha_j = (w_j / (qn - y_j)) / sum.
+// Returns the denominator (NaN/inf if ill-defined), the sum of |terms| and the
+// Lebesgue sum of the double weights (inf if the denominator is not finite).
+ld bary_eval(const ld* w, const ld* y, int m, ld qn, double* alpha, ld* sumabs, ld* lebesgue) {
+    ld tmp[256];
+    ld den = 0.0L, comp = 0.0L, sa = 0.0L;
+    for (int j = 0; j < m; ++j) {
+        const ld v = w[j] / (qn - y[j]);
+        tmp[j] = v;
+        sa += std::fabs(v);
+        const ld t = den + v;
+        if (std::fabs(den) >= std::fabs(v)) comp += (den - t) + v;
+        else comp += (v - t) + den;
+        den = t;
+    }
+    den += comp;
+    *sumabs = sa;
+    *lebesgue = std::numeric_limits<ld>::infinity();
+    if (den == den && std::isfinite(den)) {
+        const ld inv = 1.0L / den;
+        ld leb = 0.0L;
+        for (int j = 0; j < m; ++j) {
+            const double a = (double)(tmp[j] * inv);
+            alpha[j] = a;
+            leb += std::fabs(a);
+        }
+        *lebesgue = leb;
+    }
+    return den;
+}
+
+// Order-d Floater-Hormann stencils on m-point windows; the polynomial stencil
+// of the same window where FH cancels (|den| <= 1e-10 sum |terms|) or has a
+// Lebesgue sum more than twice the polynomial's.
+void stencils_fh(const std::vector<ld>& x, const std::vector<ld>& xq, int d, int m, int64_t* inds, double* w) {
+    const long long Q = (long long)xq.size();
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < Q; ++k) {
+        const ld q = xq[k];
+        const int start = window_start(x, m, q);
+        ld xn[256], yn[256], wl[256];
+        for (int j = 0; j < m; ++j) xn[j] = x[start + j];
+        double* out = w + (size_t)k * m;
+        inds[k] = start;
+        const ld span = xn[m - 1] - xn[0];
+        const ld tol = 64 * std::numeric_limits<ld>::epsilon() * (span > 0.0L ? span : 1.0L);
+        int hit = -1;
+        for (int j = 0; j < m; ++j) if (std::fabs(q - xn[j]) <= tol) { hit = j; break; }
+        if (hit >= 0) {
+            for (int j = 0; j < m; ++j) out[j] = 0.0;
+            out[hit] = 1.0;
+            continue;
+        }
+        const ld a = xn[0], b = xn[m - 1], c = 0.5L * (a + b);
+        ld sc = b - a;
+        if (sc <= 0.0L) sc = 1.0L;
+        for (int j = 0; j < m; ++j) yn[j] = (xn[j] - c) / sc;
+        const ld qn = (q - c) / sc;
+        double afh[256], apl[256];
+        for (int j = 0; j < m; ++j) afh[j] = apl[j] = 0.0;
+        ld sa_fh, leb_fh, sa_pl, leb_pl;
+        fh_node_weights(yn, m, d, wl);
+        const ld den_fh = bary_eval(wl, yn, m, qn, afh, &sa_fh, &leb_fh);
+        for (int j = 0; j < m; ++j) {
+            ld den = 1.0L;
+            for (int l = 0; l < m; ++l) if (l != j) den *= (yn[j] - yn[l]);
+            wl[j] = 1.0L / den;
+        }
+        bary_eval(wl, yn, m, qn, apl, &sa_pl, &leb_pl);
+        const ld inf = std::numeric_limits<ld>::infinity();
+        bool poly = !(den_fh == den_fh) || !std::isfinite(den_fh) || (sa_fh > 0.0L && std::fabs(den_fh) <= 1e-10L * sa_fh);
+        if (!poly && leb_pl < inf && leb_fh < inf && leb_fh > 2.0L * leb_pl) poly = true;
+        for (int j = 0; j < m; ++j) out[j] = poly ? apl[j] : afh[j];
+    }
+}
+
 // grid_io.cpp writes long-double grids at 17 digits after the point;
 // io_input.cpp reads them back as double.
 double text_trip(ld v) {
@@ -261,12 +364,19 @@ double text_trip(ld v) {
 
 }  // namespace
 
-extern "C" dyn_status dyn_grid_generate(size_t len, double Tmax, int spline_order, int interp_order, double alpha,
-                                        double delta, double* theta, double* phi1, double* phi2, double* integ,
-                                        int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2,
-                                        double* wB2) {
+// The generator behind both entry points: rational = false is -m poly
+// (depth interp_order + 1), true is -m rational (depth fh_depth(...)).
+static dyn_status generate(size_t len, double Tmax, int spline_order, int interp_order, bool rational, int fh_window,
+                           double alpha, double delta, double* theta, double* phi1, double* phi2, double* integ,
+                           int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2, double* wB2) {
     const int n = std::max(1, interp_order);
     if (len < (size_t)(n + 1) || len > 8192 || !(Tmax > 0)) return DYN_ERR_INVALID;
+    const int mfh = (int)std::min<size_t>(len, (size_t)std::max(n + 1, fh_window > 0 ? fh_window : n + 1));
+    if (rational && mfh > 256) return DYN_ERR_INVALID;
+    auto tables = [&](const std::vector<ld>& th, const std::vector<ld>& q, int64_t* inds, double* w) {
+        if (rational) stencils_fh(th, q, n, mfh, inds, w);
+        else stencils(th, q, n, inds, w);
+    };
     try {
         const std::vector<ld> th = theta_grid(len, Tmax, alpha, delta);
         const size_t N = len, N2 = N * N;
@@ -295,11 +405,33 @@ extern "C" dyn_status dyn_grid_generate(size_t len, double Tmax, int spline_orde
             if (phi1) phi1[k] = text_trip(p1[k]);
             phi2[k] = text_trip(p2[k]);
         }
-        stencils(th, p1, n, indsA1, wA1);
-        stencils(th, p2, n, indsA2, wA2);
-        stencils(th, xb, n, indsB2, wB2);
+        tables(th, p1, indsA1, wA1);
+        tables(th, p2, indsA2, wA2);
+        tables(th, xb, indsB2, wB2);
     } catch (...) {
         return DYN_ERR_INVALID;
     }
     return DYN_OK;
+}
+
+extern "C" dyn_status dyn_grid_generate(size_t len, double Tmax, int spline_order, int interp_order, double alpha,
+                                        double delta, double* theta, double* phi1, double* phi2, double* integ,
+                                        int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2,
+                                        double* wB2) {
+    return generate(len, Tmax, spline_order, interp_order, false, 0, alpha, delta, theta, phi1, phi2, integ, indsA1,
+                    wA1, indsA2, wA2, indsB2, wB2);
+}
+
+extern "C" int dyn_grid_rational_depth(size_t len, int interp_order, int fh_window) {
+    const int n = std::max(1, interp_order);
+    return (int)std::min<size_t>(len, (size_t)std::max(n + 1, fh_window > 0 ? fh_window : n + 1));
+}
+
+extern "C" dyn_status dyn_grid_generate_rational(size_t len, double Tmax, int spline_order, int interp_order,
+                                                 int fh_window, double alpha, double delta, double* theta,
+                                                 double* phi1, double* phi2, double* integ, int64_t* indsA1,
+                                                 double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2,
+                                                 double* wB2) {
+    return generate(len, Tmax, spline_order, interp_order, true, fh_window, alpha, delta, theta, phi1, phi2, integ,
+                    indsA1, wA1, indsA2, wA2, indsB2, wB2);
 }

@@ -38,20 +38,32 @@ _CACHE: dict = {}
 
 
 def generate(L: int, Tmax: float = 1e5, spline_order: int = 5, interp_order: int = 9,
-             alpha: float = 0.0, delta: float = 0.0, cache: bool = True) -> Grid:
-    key = (L, Tmax, spline_order, interp_order, alpha, delta)
+             alpha: float = 0.0, delta: float = 0.0, cache: bool = True, method: str = "poly",
+             fh_window: int = 0) -> Grid:
+    """`RG-Evo grid -L L -M Tmax -s spline_order -m method -o interp_order [-f fh_window]`:
+    method "poly" (local barycentric, depth interp_order + 1) or "rational" (local
+    Floater-Hormann of order interp_order on windows of max(interp_order + 1, fh_window)
+    points).  The reference's "bspline" tables (global weights, start index -1) are
+    metadata its own solver cannot read, so they are not generated."""
+    if method not in ("poly", "rational"):
+        raise ValueError(f"unknown stencil method {method!r} (poly | rational)")
+    key = (L, Tmax, spline_order, interp_order, alpha, delta, method, fh_window)
     if cache and key in _CACHE:
         return _CACHE[key]
-    m = interp_order + 1
+    rational = method == "rational"
+    m = _lib.lib().dyn_grid_rational_depth(L, interp_order, fh_window) if rational else interp_order + 1
     L2 = L * L
     th, it = np.empty(L), np.empty(L)
     p1, p2 = np.empty(L2), np.empty(L2)
     i1, i2, i3 = (np.empty(L2, dtype=np.int64) for _ in range(3))
     w1, w2, w3 = (np.empty(L2 * m) for _ in range(3))
     i64 = lambda a: a.ctypes.data_as(_lib.i64p)
-    st = _lib.lib().dyn_grid_generate(L, Tmax, spline_order, interp_order, alpha, delta, _lib.ptr(th), _lib.ptr(p1),
-                                      _lib.ptr(p2), _lib.ptr(it), i64(i1), _lib.ptr(w1), i64(i2), _lib.ptr(w2),
-                                      i64(i3), _lib.ptr(w3))
+    tail = (_lib.ptr(th), _lib.ptr(p1), _lib.ptr(p2), _lib.ptr(it), i64(i1), _lib.ptr(w1), i64(i2), _lib.ptr(w2),
+            i64(i3), _lib.ptr(w3))
+    if rational:
+        st = _lib.lib().dyn_grid_generate_rational(L, Tmax, spline_order, interp_order, fh_window, alpha, delta, *tail)
+    else:
+        st = _lib.lib().dyn_grid_generate(L, Tmax, spline_order, interp_order, alpha, delta, *tail)
     _lib.check(st, "dyn_grid_generate")
     g = Grid(L, th, p1, p2, it, i1, w1, i2, w2, i3, w3)
     if cache:

@@ -452,6 +452,17 @@ dyn_status dyn_grid_generate(size_t len, double Tmax, int spline_order, int inte
                              double delta, double* theta, double* phi1, double* phi2, double* integ,
                              int64_t* indsA1y, double* weightsA1y, int64_t* indsA2y, double* weightsA2y,
                              int64_t* indsB2y, double* weightsB2y);
+/* `RG-Evo grid ... -m rational -o interp_order -f fh_window`: local Floater-Hormann
+ * stencils of order interp_order on windows of dyn_grid_rational_depth(len,
+ * interp_order, fh_window) = min(len, max(interp_order + 1, fh_window)) points
+ * (compute_barycentric_rational_weights, interpolation_weights.cpp:159-280), the
+ * polynomial stencil of the window where FH is ill-conditioned.  The weight arrays
+ * hold that depth per target; the depth is at most 256. */
+int dyn_grid_rational_depth(size_t len, int interp_order, int fh_window);
+dyn_status dyn_grid_generate_rational(size_t len, double Tmax, int spline_order, int interp_order, int fh_window,
+                                      double alpha, double delta, double* theta, double* phi1, double* phi2,
+                                      double* integ, int64_t* indsA1y, double* weightsA1y, int64_t* indsA2y,
+                                      double* weightsA2y, int64_t* indsB2y, double* weightsB2y);
 
 #ifdef __cplusplus
 }

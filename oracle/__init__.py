@@ -333,6 +333,8 @@ class Reference:
                                          C.c_double, C.c_double, C.c_int]
             lib.dynref_set_tables.argtypes = [_dp, _dp, _dp, _dp, _i64p, _i64p, _i64p, _dp, _dp, _dp, C.c_size_t]
             lib.dynref_set_log_response.argtypes = [C.c_int]
+            lib.dynref_grid_method.argtypes = [C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
+                                               C.c_double, _dp, _dp, _dp, _dp, _i64p, _dp, _i64p, _dp, _i64p, _dp]
             lib.dynref_set_tail_fit.argtypes = [C.c_int]
             lib.dynref_set_rollback_loop.argtypes = [C.c_int]
             lib.dynref_init_state.argtypes = [C.c_double]
@@ -376,16 +378,17 @@ class Reference:
 
     @classmethod
     def grid(cls, L: int, Tmax: float = 1e5, spline_order: int = 5, interp_order: int = 9,
-             alpha: float = 0.0, delta: float = 0.0) -> Grid:
+             alpha: float = 0.0, delta: float = 0.0, method: str = "poly", fh_window: int = 0) -> Grid:
         lib = cls.lib()
-        m = interp_order + 1
+        n = max(1, interp_order)
+        m = min(L, max(n + 1, fh_window if fh_window > 0 else n + 1)) if method == "rational" else n + 1
         L2 = L * L
         th, p1, p2, it = np.empty(L), np.empty(L2), np.empty(L2), np.empty(L)
         i1, i2, i3 = (np.empty(L2, dtype=np.int64) for _ in range(3))
         w1, w2, w3 = (np.empty(L2 * m) for _ in range(3))
-        lib.dynref_grid(L, Tmax, spline_order, interp_order, alpha, delta, _d(th), _d(p1), _d(p2), _d(it),
-                        i1.ctypes.data_as(_i64p), _d(w1), i2.ctypes.data_as(_i64p), _d(w2),
-                        i3.ctypes.data_as(_i64p), _d(w3))
+        lib.dynref_grid_method(L, Tmax, spline_order, interp_order, fh_window if method == "rational" else -1, alpha,
+                               delta, _d(th), _d(p1), _d(p2), _d(it), i1.ctypes.data_as(_i64p), _d(w1),
+                               i2.ctypes.data_as(_i64p), _d(w2), i3.ctypes.data_as(_i64p), _d(w3))
         return Grid(L, th, p1, p2, it, i1, w1, i2, w2, i3, w3)
 
     def init_state(self, delta_t: float = 0.0):

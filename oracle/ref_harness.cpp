@@ -10,6 +10,7 @@
 // The few pieces of driver logic that live in files not compiled here
 // (t=0 state, controller, CPU energy) are restated with citations.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -340,10 +341,25 @@ double dynref_spec_rad(void) { return config.specRad; }
 
 // Grid generation: the same calls and post-processing as grid_cli.cpp:78-215
 // (poly method), returning the values the solver reads back from the files.
+// grid_cli.cpp:84-215 for -m poly (fh_window < 0) or -m rational (window size
+// min(len, max(n + 1, fh_window)), fh_window 0: n + 1); weights hold that depth
+int dynref_grid_method(size_t len, double Tmax, int spline_order, int interp_order, int fh_window, double alpha,
+                       double delta, double* theta, double* phi1, double* phi2, double* integ,
+                       int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2,
+                       double* wB2);
+
 int dynref_grid(size_t len, double Tmax, int spline_order, int interp_order, double alpha,
                 double delta, double* theta, double* phi1, double* phi2, double* integ,
                 int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2,
                 double* wB2) {
+    return dynref_grid_method(len, Tmax, spline_order, interp_order, -1, alpha, delta, theta, phi1, phi2, integ,
+                              indsA1, wA1, indsA2, wA2, indsB2, wB2);
+}
+
+int dynref_grid_method(size_t len, double Tmax, int spline_order, int interp_order, int fh_window, double alpha,
+                       double delta, double* theta, double* phi1, double* phi2, double* integ,
+                       int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2,
+                       double* wB2) {
     std::vector<long double> th;
     generate_theta_grid(len, Tmax, th, alpha, delta);
     std::vector<long double> p1, p2;
@@ -352,15 +368,21 @@ int dynref_grid(size_t len, double Tmax, int spline_order, int interp_order, dou
     compute_integration_weights(th, spline_order, wint);
     const size_t N = len;
     const int n = interp_order < 1 ? 1 : interp_order;
-    const int m = n + 1;
+    const bool rational = fh_window >= 0;
+    const int mfh = (int)std::min<size_t>(N, (size_t)std::max(n + 1, fh_window > 0 ? fh_window : n + 1));
+    const int m = rational ? mfh : n + 1;
+    auto weights = [&](const std::vector<long double>& q) {
+        return rational ? dmfe::grid::compute_barycentric_rational_weights(th, q, n, mfh)
+                        : dmfe::grid::compute_barycentric_weights(th, q, n);
+    };
     for (size_t i = 0; i < N; ++i) theta[i] = static_cast<double>(th[i]);
     for (size_t i = 0; i < N; ++i) integ[i] = static_cast<double>(wint[i]);
     for (size_t k = 0; k < N * N; ++k) {
         phi1[k] = text_round_trip(p1[k]);
         phi2[k] = text_round_trip(p2[k]);
     }
-    auto st1 = dmfe::grid::compute_barycentric_weights(th, p1, n);
-    auto st2 = dmfe::grid::compute_barycentric_weights(th, p2, n);
+    auto st1 = weights(p1);
+    auto st2 = weights(p2);
     const double tiny = 1e-200;
     std::vector<long double> xqB2;
     xqB2.reserve(N * N);
@@ -374,7 +396,7 @@ int dynref_grid(size_t len, double Tmax, int spline_order, int interp_order, dou
             xqB2.push_back(arg);
         }
     }
-    auto st3 = dmfe::grid::compute_barycentric_weights(th, xqB2, n);
+    auto st3 = weights(xqB2);
     for (size_t k = 0; k < N * N; ++k) {
         indsA1[k] = st1[k].start;
         indsA2[k] = st2[k].start;

@@ -42,6 +42,36 @@ def test_generator_invariants(product_built):
         assert np.max(np.abs(approx - xq ** d)) < 5e-13, d
 
 
+@pytest.mark.parametrize("L,order,window", [(64, 9, 0), (80, 5, 12), (128, 9, 14)])
+def test_rational_generator_matches_reference(product_built, oracle_built, L, order, window):
+    """-m rational (Floater-Hormann stencils, grid_cli.cpp:104-141, 198-206) against the
+    reference generator compiled here: every table bit for bit."""
+    import oracle as O
+    if not O.Reference.available():
+        pytest.skip("compiled reference not present")
+    g = product_built.grid.generate(L, Tmax=1e3, interp_order=order, method="rational", fh_window=window,
+                                    cache=False)
+    r = O.Reference.grid(L, Tmax=1e3, interp_order=order, method="rational", fh_window=window)
+    assert g.depth == max(order + 1, window)
+    for f in FIELDS:
+        np.testing.assert_array_equal(getattr(g, f), getattr(r, f), err_msg=f)
+
+
+def test_rational_stencils_reproduce_low_degree_polynomials(product_built):
+    """A Floater-Hormann interpolant of order d reproduces polynomials of degree <= d
+    (and the polynomial fallback, of degree m - 1 >= d, does too)."""
+    L, d = 96, 5
+    g = product_built.grid.generate(L, Tmax=1e3, interp_order=d, method="rational", fh_window=12, cache=False)
+    m = g.depth
+    w = g.wA2.reshape(L * L, m)
+    idx = g.indsA2[:, None] + np.arange(m)[None, :]
+    np.testing.assert_allclose(w.sum(axis=1), 1.0, atol=1e-13)
+    for k in range(1, d + 1):
+        assert np.max(np.abs((w * g.theta[idx] ** k).sum(axis=1) - g.phi2 ** k)) < 1e-11, k
+    with pytest.raises(ValueError):
+        product_built.grid.generate(32, method="bspline")
+
+
 def test_text_format_round_trip(product_built, tmp_path):
     g = product_built.grid.generate(32, Tmax=10.0, cache=False)
     product_built.grid.save(g, str(tmp_path))

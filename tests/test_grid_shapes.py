@@ -1,6 +1,7 @@
 """Grid shapes other than the golden poly-9 grids: stencil depth 8 (interp_order 7)
-at L = 72 (partial tiles in the gather and the epilogue) and depth 6
-(interp_order 5) at L = 96, both from the native generator (bit-identical to the
+at L = 72 (partial tiles in the gather and the epilogue), depth 6 (interp_order 5)
+at L = 96, and Floater-Hormann (-m rational) stencils of order 5 on 12-point
+windows at L = 80, all from the native generator (bit-identical to the
 reference's).  They take the generic-depth instantiations of every kernel family
 (FP64 and mixed gathers, the batch, the log-space form, the adjoint's generic B2
 path), which the depth-10 golden cases never reach.
@@ -15,13 +16,16 @@ import pytest
 import oracle as O
 from helpers import rel_err
 
-SHAPES = [(72, 7), (96, 5)]
+SHAPES = [(72, 7), (96, 5), (80, -5)]  # a negative order: -m rational, FH order 5 on 12-point windows
 STEPS = 60
 
 
 def _grids(L, order):
     import dynamite_gb300 as D
-    g = D.grid.generate(L, Tmax=1e3, interp_order=order)
+    if order < 0:
+        g = D.grid.generate(L, Tmax=1e3, interp_order=-order, method="rational", fh_window=12)
+    else:
+        g = D.grid.generate(L, Tmax=1e3, interp_order=order)
     og = O.Grid(L, g.theta, g.phi1, g.phi2, g.integ, g.indsA1, g.wA1, g.indsA2, g.wA2, g.indsB2, g.wB2)
     return g, og
 
@@ -35,7 +39,8 @@ def test_oracle_matches_reference_on_other_depths(product_built, oracle_built, L
         pytest.skip("compiled reference not present")
     import dynamite_gb300 as D
     g, og = _grids(L, order)
-    ref_grid = O.Reference.grid(L, Tmax=1e3, interp_order=order)
+    ref_grid = (O.Reference.grid(L, Tmax=1e3, interp_order=-order, method="rational", fh_window=12) if order < 0
+                else O.Reference.grid(L, Tmax=1e3, interp_order=order))
     for f in ("theta", "indsA1", "wA1", "indsB2", "wB2"):
         np.testing.assert_array_equal(getattr(g, f), getattr(ref_grid, f), err_msg=f)
     p = O.Port(og, O.Model(**MODEL), search_mode=0, threads=4)
@@ -48,7 +53,7 @@ def test_oracle_matches_reference_on_other_depths(product_built, oracle_built, L
     np.testing.assert_array_equal(a.t1grid, b.t1grid)
     np.testing.assert_array_equal(a.QK, b.QK)
     np.testing.assert_array_equal(tp["energy"], tr["energy"])
-    assert g.depth == order + 1 and np.isfinite(a.QK).all()
+    assert g.depth == (12 if order < 0 else order + 1) and np.isfinite(a.QK).all()
 
 
 @pytest.mark.gpu
