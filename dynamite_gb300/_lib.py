@@ -195,6 +195,7 @@ def lib():
             "dyn_grid_generate": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                    dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
             "dyn_grid_rational_depth": ([C.c_size_t, C.c_int, C.c_int], C.c_int),
+            "dyn_grid_positions": ([C.c_size_t, C.c_double, C.c_double, C.c_double, dp, dp, dp], C.c_int),
             "dyn_grid_generate_rational": ([C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                             dp, dp, dp, dp, i64p, dp, i64p, dp, i64p, dp], C.c_int),
         }

@@ -97,7 +97,8 @@ ld remap_index(ld x1, size_t len, double alpha, double delta) {
 
 // theta(i) = [T(1) - T(i)] / [T(L/2+) - T(L/2-)] with T(x) = (2/pi) atan(exp(-(x - L/2 - 1/2) eta)),
 // eta = -(2/L) W_{-1}(-1/(10 Tmax))   (theta_grid.cpp:37-125)
-std::vector<ld> theta_grid(size_t len, double Tmax, double alpha, double delta) {
+// theta at 0-based fractional indices (theta_of_vec, theta_grid.cpp:72-110)
+std::vector<ld> theta_at(const std::vector<double>& indices, size_t len, double Tmax, double alpha, double delta) {
     const ld Lm = (ld)len;
     const ld Wm1 = lambert_wm1(-ld(1) / (ld(10) * (ld)Tmax));
     const ld eta = -(ld(2) / Lm) * Wm1;
@@ -105,9 +106,9 @@ std::vector<ld> theta_grid(size_t len, double Tmax, double alpha, double delta) 
     const ld term_ref = (ld(2) / PI_L) * datan(ld(1) / dexp(tref));
     const ld thalf = ((Lm / ld(2)) - ld(1) / ld(2)) * eta;
     const ld den = (ld(2) / PI_L) * datan(dexp(thalf)) - (ld(2) / PI_L) * datan(dexp(-thalf));
-    std::vector<ld> th(len);
-    for (size_t k = 0; k < len; ++k) {
-        const ld x1 = remap_index((ld)(double)k + 1.0L, len, alpha, delta);
+    std::vector<ld> th(indices.size());
+    for (size_t k = 0; k < indices.size(); ++k) {
+        const ld x1 = remap_index((ld)indices[k] + 1.0L, len, alpha, delta);
         const ld idx = (ld)(double)x1;
         const ld t1 = (idx - (Lm / ld(2)) - ld(1) / ld(2)) * eta;
         const ld term1 = (ld(2) / PI_L) * datan(ld(1) / dexp(t1));
@@ -117,9 +118,79 @@ std::vector<ld> theta_grid(size_t len, double Tmax, double alpha, double delta) 
         if (v > 1.0) v = 1.0;
         th[k] = v;
     }
+    return th;
+}
+
+std::vector<ld> theta_grid(size_t len, double Tmax, double alpha, double delta) {
+    std::vector<double> idx(len);
+    for (size_t k = 0; k < len; ++k) idx[k] = (double)k;
+    std::vector<ld> th = theta_at(idx, len, Tmax, alpha, delta);
     for (size_t k = 1; k < len; ++k)
         if (th[k] < th[k - 1]) th[k] = th[k - 1];
     return th;
+}
+
+// ---- position grids (pos_grid.cpp:111-205): the inverse map theta -> 1-based
+// fractional index, as a local barycentric interpolant of m = 12 nodes through
+// theta sampled at 20 len points, evaluated at phi1, phi2 and theta_i / phi2 ----
+struct InverseTheta {
+    std::vector<ld> x, y;  // theta samples (strictly increasing), 1-based positions
+    std::vector<int> left;  // first node of the window of interval i
+    std::vector<ld> w;      // barycentric weights of every window start
+    int m = 12;
+
+    void build(size_t len, double Tmax, double alpha, double delta, size_t oversample, int m_req) {
+        const size_t M = len * oversample;
+        std::vector<double> idx(M);
+        y.resize(M);
+        for (size_t k = 0; k < M; ++k) {
+            y[k] = 1.0L + ((ld)len - 1.0L) * ((ld)k / (ld)(M - 1));
+            idx[k] = (double)(y[k] - 1.0L);
+        }
+        x = theta_at(idx, len, Tmax, alpha, delta);
+        for (size_t k = 1; k < M; ++k)
+            if (x[k] <= x[k - 1]) x[k] = std::nextafter(x[k - 1], std::numeric_limits<ld>::infinity());
+        m = std::max(4, std::min(16, m_req));
+        if (m > (int)M) m = (int)M;
+        const int Nm = (int)M - m, nleft = std::max(0, Nm) + 1;
+        left.resize(M - 1);
+        for (size_t i = 0; i + 1 < M; ++i) left[i] = std::min(std::max((int)i - m / 2 + 1, 0), std::max(0, Nm));
+        w.assign((size_t)nleft * m, 0.0L);
+        for (int L0 = 0; L0 < nleft; ++L0)
+            for (int j = 0; j < m; ++j) {
+                ld prod = 1.0L;
+                for (int k = 0; k < m; ++k)
+                    if (k != j) prod *= x[(size_t)(L0 + j)] - x[(size_t)(L0 + k)];
+                w[(size_t)L0 * m + j] = 1.0L / prod;
+            }
+    }
+
+    ld operator()(ld v) const {
+        if (v <= x.front()) return y.front();
+        if (v >= x.back()) return y.back();
+        const size_t i = std::max<size_t>(1, (size_t)(std::upper_bound(x.begin(), x.end(), v) - x.begin())) - 1;
+        const int nleft = std::max(0, (int)x.size() - m) + 1;
+        const int L0 = std::min(std::max(left[i], 0), nleft - 1);
+        const ld* wp = &w[(size_t)L0 * m];
+        for (int j = 0; j < m; ++j)
+            if (v == x[(size_t)(L0 + j)]) return y[(size_t)(L0 + j)];
+        ld num = 0.0L, den = 0.0L;
+        for (int j = 0; j < m; ++j) {
+            const ld q = wp[j] / (v - x[(size_t)(L0 + j)]);
+            den += q;
+            num += q * y[(size_t)(L0 + j)];
+        }
+        return num / den;
+    }
+};
+
+// the reference reads these two tuning variables (clamped the same way)
+size_t env_size(const char* name, size_t def, long lo) {
+    if (const char* e = std::getenv(name)) {
+        const long v = std::strtol(e, nullptr, 10);
+        if (v > lo) return (size_t)v;
+    }
+    return def;
 }
 
 // ---- integration weights: spline-consistent quadrature (integration.cpp) ----
@@ -420,6 +491,36 @@ extern "C" dyn_status dyn_grid_generate(size_t len, double Tmax, int spline_orde
                                         double* wB2) {
     return generate(len, Tmax, spline_order, interp_order, false, 0, alpha, delta, theta, phi1, phi2, integ, indsA1,
                     wA1, indsA2, wA2, indsB2, wB2);
+}
+
+extern "C" dyn_status dyn_grid_positions(size_t len, double Tmax, double alpha, double delta, double* posA1y,
+                                         double* posA2y, double* posB2y) {
+    if (len < 4 || len > 8192 || !(Tmax > 0) || !posA1y || !posA2y || !posB2y) return DYN_ERR_INVALID;
+    try {
+        const std::vector<ld> th = theta_grid(len, Tmax, alpha, delta);
+        InverseTheta inv;
+        int m_req = 12;
+        if (const char* e = std::getenv("DMFE_POS_BARY_M")) m_req = std::max(2, std::min(32, (int)std::strtol(e, nullptr, 10)));
+        inv.build(len, Tmax, alpha, delta, env_size("DMFE_POS_OVERSAMPLE", 20, 1), m_req);
+        const ld tmin = inv.x.front(), tmax = inv.x.back(), tiny = 1e-200L;
+        const size_t N = len;
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < (long long)N; ++i) {
+            const ld ti = th[(size_t)i], omt = 1.0L - ti;
+            for (size_t j = 0; j < N; ++j) {
+                const size_t k = (size_t)i * N + j;
+                const ld v1 = ti * th[j], v2 = ti + omt * th[j];
+                posA1y[k] = (double)inv(v1);
+                posA2y[k] = (double)inv(v2);
+                const ld den = v2 - tiny;
+                const ld arg = std::fabs(den) < 1e-300L ? (ti > 0 ? tmax : tmin) : ti / den;
+                posB2y[k] = (double)inv(arg);
+            }
+        }
+    } catch (...) {
+        return DYN_ERR_INVALID;
+    }
+    return DYN_OK;
 }
 
 extern "C" int dyn_grid_rational_depth(size_t len, int interp_order, int fh_window) {

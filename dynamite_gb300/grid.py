@@ -1,9 +1,11 @@
 """Stencil/quadrature tables: generation (native) and the RG-Evo text format.
 
-`generate` is the reference's `RG-Evo grid` (grid_cli.cpp:35-258, poly
-method) done by the native generator in the library; `load`/`save` read and
-write `Grid_data/<L>/` as the reference does (io_input.cpp:90-110,
-grid_io.cpp:26-263), so tables interchange with RG-Evo in both directions.
+`generate` is the reference's `RG-Evo grid` (grid_cli.cpp:35-258, poly and
+rational methods) done by the native generator in the library; `load`/`save`
+read and write `Grid_data/<L>/` as the reference does (io_input.cpp:90-110,
+grid_io.cpp:26-263, with the position grids and grid_params.txt the reference
+checks for, initialization.cpp:40-62), so tables interchange with RG-Evo in both
+directions.
 """
 from __future__ import annotations
 
@@ -28,6 +30,7 @@ class Grid:
     wA2: np.ndarray
     indsB2: np.ndarray
     wB2: np.ndarray
+    params: dict | None = None  # generation parameters (set by generate)
 
     @property
     def depth(self) -> int:
@@ -65,10 +68,21 @@ def generate(L: int, Tmax: float = 1e5, spline_order: int = 5, interp_order: int
     else:
         st = _lib.lib().dyn_grid_generate(L, Tmax, spline_order, interp_order, alpha, delta, *tail)
     _lib.check(st, "dyn_grid_generate")
-    g = Grid(L, th, p1, p2, it, i1, w1, i2, w2, i3, w3)
+    params = dict(len=L, Tmax=Tmax, spline_order=spline_order, interp_method=method, interp_order=max(1, interp_order),
+                  fh_stencil=m if rational else 0, alpha=alpha, delta=delta)
+    g = Grid(L, th, p1, p2, it, i1, w1, i2, w2, i3, w3, params)
     if cache:
         _CACHE[key] = g
     return g
+
+
+def positions(L: int, Tmax: float = 1e5, alpha: float = 0.0, delta: float = 0.0):
+    """posA1y, posA2y, posB2y (generate_pos_grids, pos_grid.cpp:111-205): the 1-based
+    fractional theta index of phi1, phi2 and theta_i / phi2, each L*L."""
+    out = [np.empty(L * L) for _ in range(3)]
+    _lib.check(_lib.lib().dyn_grid_positions(L, Tmax, alpha, delta, *[_lib.ptr(a) for a in out]),
+               "dyn_grid_positions")
+    return tuple(out)
 
 
 def _read(path: str, dtype=np.float64) -> np.ndarray:
@@ -106,6 +120,21 @@ def save(g: Grid, directory: str) -> None:
     for name, inds, w in (("A1y", g.indsA1, g.wA1), ("A2y", g.indsA2, g.wA2), ("B2y", g.indsB2, g.wB2)):
         mat(f"inds{name}.dat", inds, fmt="%d")
         vec(f"weights{name}.dat", w)
+    if g.params is None:
+        return
+    # the position grids and the provenance file (grid_io.cpp:159-228)
+    p = g.params
+    for name, a in zip(("posA1y.dat", "posA2y.dat", "posB2y.dat"), positions(L, p["Tmax"], p["alpha"], p["delta"])):
+        mat(name, a)
+    lines = ["# DYNAMITE grid generation parameters", f"len={L}", f"Tmax={p['Tmax']:.17e}",
+             f"spline_order={p['spline_order']}", f"interp_method={p['interp_method']}",
+             f"interp_order={p['interp_order']}"]
+    if p["fh_stencil"] > 0:
+        lines.append(f"fh_stencil={p['fh_stencil']}")
+    lines += [f"alpha={p['alpha']:.17e}", f"delta={p['delta']:.17e}",
+              f"subdir={os.path.basename(os.path.normpath(directory))}"]
+    with open(os.path.join(directory, "grid_params.txt"), "w") as fh:
+        fh.write("\n".join(lines) + "\n")
 
 
 def lagrange_weights(theta, x: float, npts: int = 10):

@@ -459,6 +459,12 @@ dyn_status dyn_grid_generate(size_t len, double Tmax, int spline_order, int inte
  * polynomial stencil of the window where FH is ill-conditioned.  The weight arrays
  * hold that depth per target; the depth is at most 256. */
 int dyn_grid_rational_depth(size_t len, int interp_order, int fh_window);
+/* The position grids RG-Evo's Grid_data holds beside the tables (posA1y.dat,
+ * posA2y.dat, posB2y.dat; generate_pos_grids, pos_grid.cpp:111-205): the
+ * 1-based fractional theta index of phi1, phi2 and theta_i / phi2, each len*len.
+ * The solver does not read them; the reference checks that they exist. */
+dyn_status dyn_grid_positions(size_t len, double Tmax, double alpha, double delta, double* posA1y, double* posA2y,
+                              double* posB2y);
 dyn_status dyn_grid_generate_rational(size_t len, double Tmax, int spline_order, int interp_order, int fh_window,
                                       double alpha, double delta, double* theta, double* phi1, double* phi2,
                                       double* integ, int64_t* indsA1y, double* weightsA1y, int64_t* indsA2y,

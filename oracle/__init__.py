@@ -333,6 +333,7 @@ class Reference:
                                          C.c_double, C.c_double, C.c_int]
             lib.dynref_set_tables.argtypes = [_dp, _dp, _dp, _dp, _i64p, _i64p, _i64p, _dp, _dp, _dp, C.c_size_t]
             lib.dynref_set_log_response.argtypes = [C.c_int]
+            lib.dynref_grid_positions.argtypes = [C.c_size_t, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]
             lib.dynref_grid_method.argtypes = [C.c_size_t, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double,
                                                C.c_double, _dp, _dp, _dp, _dp, _i64p, _dp, _i64p, _dp, _i64p, _dp]
             lib.dynref_set_tail_fit.argtypes = [C.c_int]
@@ -390,6 +391,13 @@ class Reference:
                                delta, _d(th), _d(p1), _d(p2), _d(it), i1.ctypes.data_as(_i64p), _d(w1),
                                i2.ctypes.data_as(_i64p), _d(w2), i3.ctypes.data_as(_i64p), _d(w3))
         return Grid(L, th, p1, p2, it, i1, w1, i2, w2, i3, w3)
+
+    @classmethod
+    def grid_positions(cls, L: int, Tmax: float = 1e5, alpha: float = 0.0, delta: float = 0.0):
+        """posA1y, posA2y, posB2y as the reference generator writes them."""
+        out = [np.empty(L * L) for _ in range(3)]
+        cls.lib().dynref_grid_positions(L, Tmax, alpha, delta, *[_d(a) for a in out])
+        return tuple(out)
 
     def init_state(self, delta_t: float = 0.0):
         self.lib().dynref_init_state(delta_t)

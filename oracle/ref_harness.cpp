@@ -33,6 +33,7 @@
 #include "search/search_utils.hpp"
 #include "grid/theta_grid.hpp"
 #include "grid/phi_grid.hpp"
+#include "grid/pos_grid.hpp"
 #include "grid/integration.hpp"
 #include "grid/interpolation_weights.hpp"
 
@@ -347,6 +348,20 @@ int dynref_grid_method(size_t len, double Tmax, int spline_order, int interp_ord
                        double delta, double* theta, double* phi1, double* phi2, double* integ,
                        int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2,
                        double* wB2);
+
+// generate_pos_grids (pos_grid.cpp:111-205) on the generator's theta and phi grids
+int dynref_grid_positions(size_t len, double Tmax, double alpha, double delta, double* posA1y, double* posA2y,
+                          double* posB2y) {
+    std::vector<long double> th, p1, p2;
+    generate_theta_grid(len, Tmax, th, alpha, delta);
+    generate_phi_grids(th, p1, p2);
+    std::vector<double> a1, a2, b2;
+    generate_pos_grids(len, Tmax, th, p1, p2, a1, a2, b2, alpha, delta);
+    std::copy(a1.begin(), a1.end(), posA1y);
+    std::copy(a2.begin(), a2.end(), posA2y);
+    std::copy(b2.begin(), b2.end(), posB2y);
+    return 0;
+}
 
 int dynref_grid(size_t len, double Tmax, int spline_order, int interp_order, double alpha,
                 double delta, double* theta, double* phi1, double* phi2, double* integ,

@@ -72,6 +72,41 @@ def test_rational_stencils_reproduce_low_degree_polynomials(product_built):
         product_built.grid.generate(32, method="bspline")
 
 
+@pytest.mark.parametrize("L,Tmax,alpha,delta", [(32, 10.0, 0.0, 0.0), (128, 1e5, 0.0, 0.0), (96, 1e3, 0.3, 0.2)])
+def test_position_grids_match_reference(product_built, oracle_built, L, Tmax, alpha, delta):
+    """posA1y/posA2y/posB2y (pos_grid.cpp:111-205, the inverse theta map through 20 L
+    samples and 12-node barycentric windows) bit for bit, with and without the
+    index remap (alpha, delta)."""
+    import oracle as O
+    if not O.Reference.available():
+        pytest.skip("compiled reference not present")
+    ours = product_built.grid.positions(L, Tmax, alpha, delta)
+    ref = O.Reference.grid_positions(L, Tmax, alpha, delta)
+    for a, b, name in zip(ours, ref, ("posA1y", "posA2y", "posB2y")):
+        np.testing.assert_array_equal(a, b, err_msg=name)
+
+
+def test_saved_grid_directory_is_complete(product_built, tmp_path):
+    """save() of a generated grid writes every file the reference's solver checks for
+    before it runs (initialization.cpp:40-62) and grid_params.txt (grid_io.cpp:205-228)."""
+    G = product_built.grid
+    g = G.generate(32, Tmax=10.0, method="rational", fh_window=12, cache=False)
+    d = tmp_path / "32"
+    G.save(g, str(d))
+    for f in ("theta.dat", "phi1.dat", "phi2.dat", "int.dat", "indsA1y.dat", "weightsA1y.dat", "indsA2y.dat",
+              "weightsA2y.dat", "indsB2y.dat", "weightsB2y.dat", "posA1y.dat", "posA2y.dat", "posB2y.dat"):
+        assert (d / f).exists(), f
+    params = (d / "grid_params.txt").read_text().splitlines()
+    assert params[:2] == ["# DYNAMITE grid generation parameters", "len=32"]
+    assert "Tmax=1.00000000000000000e+01" in params and "interp_method=rational" in params
+    assert "fh_stencil=12" in params and "subdir=32" in params
+    pos = np.loadtxt(d / "posB2y.dat", delimiter="\t").ravel()
+    np.testing.assert_array_equal(pos, G.positions(32, 10.0)[2])
+    back = G.load(str(d))
+    for f in FIELDS:
+        np.testing.assert_array_equal(getattr(g, f), getattr(back, f), err_msg=f)
+
+
 def test_text_format_round_trip(product_built, tmp_path):
     g = product_built.grid.generate(32, Tmax=10.0, cache=False)
     product_built.grid.save(g, str(tmp_path))
