@@ -85,6 +85,30 @@ def positions(L: int, Tmax: float = 1e5, alpha: float = 0.0, delta: float = 0.0)
     return tuple(out)
 
 
+def validate(directory: str, L: int, Tmax: float = 1e5, spline_order: int = 5, alpha: float = 0.0,
+             delta: float = 0.0) -> dict:
+    """`RG-Evo grid -V`: regenerate theta, phi1, phi2 and int.dat and compare them with the
+    files in `directory` (phi_grid.cpp:38-72 at 5e-16, integration.cpp:208-227 at 1e-7,
+    absolute).  A missing or mis-sized file fails the check."""
+    out = dict(ok=False, max_abs_diff=np.inf, mismatches=-1, max_abs_diff_int=np.inf, mismatches_int=-1)
+    try:
+        th = _read(os.path.join(directory, "theta.dat"))
+        p1 = _read(os.path.join(directory, "phi1.dat"))
+        p2 = _read(os.path.join(directory, "phi2.dat"))
+        wi = _read(os.path.join(directory, "int.dat"))
+    except OSError:
+        return out
+    if th.size != L or p1.size != L * L or p2.size != L * L or wi.size != L:
+        return out
+    g = generate(L, Tmax, spline_order, 1, alpha, delta, cache=False)
+    d = np.abs(np.concatenate([g.theta - th, g.phi1 - p1, g.phi2 - p2]))
+    di = np.abs(g.integ - wi)
+    out.update(max_abs_diff=float(d.max()), mismatches=int((d > 5e-16).sum()), max_abs_diff_int=float(di.max()),
+               mismatches_int=int((di > 1e-7).sum()))
+    out["ok"] = out["mismatches"] == 0 and out["mismatches_int"] == 0
+    return out
+
+
 def _read(path: str, dtype=np.float64) -> np.ndarray:
     with open(path, "r") as fh:
         return np.array(fh.read().split(), dtype=dtype)

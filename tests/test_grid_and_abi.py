@@ -107,6 +107,24 @@ def test_saved_grid_directory_is_complete(product_built, tmp_path):
         np.testing.assert_array_equal(getattr(g, f), getattr(back, f), err_msg=f)
 
 
+def test_validate_mode(product_built, tmp_path):
+    """`RG-Evo grid -V` (grid_cli.cpp:235-256): a saved grid validates; a perturbed phi2 or
+    int.dat entry, or a missing file, fails."""
+    G = product_built.grid
+    g = G.generate(32, Tmax=10.0, cache=False)
+    d = tmp_path / "32"
+    G.save(g, str(d))
+    assert G.validate(str(d), 32, Tmax=10.0)["ok"]
+    assert not G.validate(str(d), 32, Tmax=100.0)["ok"]
+    phi2 = g.phi2.copy()
+    phi2[5] += 1e-12
+    np.savetxt(d / "phi2.dat", phi2.reshape(32, 32), fmt="%.17e", delimiter="\t")
+    r = G.validate(str(d), 32, Tmax=10.0)
+    assert not r["ok"] and r["mismatches"] == 1
+    (d / "int.dat").unlink()
+    assert not G.validate(str(d), 32, Tmax=10.0)["ok"]
+
+
 def test_text_format_round_trip(product_built, tmp_path):
     g = product_built.grid.generate(32, Tmax=10.0, cache=False)
     product_built.grid.save(g, str(tmp_path))
