@@ -442,6 +442,7 @@ static dyn_status generate(size_t len, double Tmax, int spline_order, int interp
                            int64_t* indsA1, double* wA1, int64_t* indsA2, double* wA2, int64_t* indsB2, double* wB2) {
     const int n = std::max(1, interp_order);
     if (len < (size_t)(n + 1) || len > 8192 || !(Tmax > 0)) return DYN_ERR_INVALID;
+    if (!theta || !phi2 || !integ || !indsA1 || !wA1 || !indsA2 || !wA2 || !indsB2 || !wB2) return DYN_ERR_INVALID;
     const int mfh = (int)std::min<size_t>(len, (size_t)std::max(n + 1, fh_window > 0 ? fh_window : n + 1));
     if (rational && mfh > 256) return DYN_ERR_INVALID;
     auto tables = [&](const std::vector<ld>& th, const std::vector<ld>& q, int64_t* inds, double* w) {

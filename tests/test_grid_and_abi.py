@@ -155,6 +155,12 @@ def test_invalid_arguments_rejected_without_touching_the_gpu(product_built):
     assert b"null" in L.dyn_last_error()
     assert L.dyn_update(None, 1, 1e-3, None) == -1
     assert L.dyn_sparsify(None, 1e-10, 0, None) == -1
+    assert L.dyn_tail_fit(None, -1000, None) == -1
+    assert L.dyn_state_time(None, None) == -1
+    # the generator: null tables and impossible sizes
+    assert L.dyn_grid_generate(32, 10.0, 5, 9, 0.0, 0.0, *([None] * 10)) == -1
+    assert L.dyn_grid_positions(2, 10.0, 0.0, 0.0, None, None, None) == -1
+    assert L.dyn_grid_rational_depth(32, 9, 40) == 32 and L.dyn_grid_rational_depth(64, 5, 0) == 6
 
 
 def test_missing_library_raises(monkeypatch, tmp_path):
