@@ -1051,6 +1051,7 @@ dyn_status dyn_energy(void* p, double* e) {
 dyn_status dyn_tail_fit(void* p, int last_rollback_loop, dyn_tail_info* info) {
     if (!p) return fail(DYN_ERR_INVALID, "null ctx");
     Ctx* c = C(p);
+    TraceRange tr("dyn_tail_fit");
     dyn_status s = tail_fit(c, last_rollback_loop);
     if (s || !info) return s;
     TailState t;
@@ -1103,12 +1104,14 @@ dyn_status dyn_update(void* p, int method, double delta_t, dyn_step_result* res)
     if (!p) return fail(DYN_ERR_INVALID, "null ctx");
     if (method < 1) return fail(DYN_ERR_INVALID, "unknown method");
     if (!(delta_t > 0.0)) return fail(DYN_ERR_INVALID, "delta_t must be positive");
+    TraceRange tr("dyn_update");
     return C(p)->step(method, delta_t, res);
 }
 
 // simulation_runner.cpp:125-304 for a fixed number of iterations
 dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
     if (!p || !rp) return fail(DYN_ERR_INVALID, "null argument");
+    TraceRange tr("dyn_run");
     Ctx* c = C(p);
     dyn_controller& k = c->ctl;
     const double dmax = c->cfg.delta_max, dmin = c->cfg.delta_t_min;
@@ -1120,6 +1123,7 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
             k.method = rp->method_schedule ? rp->method_schedule[it] : k.method;
         }
         const double t = c->t1[c->n - 1] + k.delta_t;
+        TraceRange ts("dyn_run step");
         if (rp->out_dt) rp->out_dt[it] = k.delta_t;
         if (rp->out_method) rp->out_method[it] = k.method;
         k.delta_old = k.delta;
@@ -1283,6 +1287,7 @@ dyn_status dyn_probe_fp64(int device, double* gflops) {
 // ------------------------------------------------------------------ adjoint
 dyn_status dyn_adjoint_forward(void* p, const dyn_run_params* rp, dyn_step_result* last) {
     if (!p || !rp) return fail(DYN_ERR_INVALID, "null argument");
+    TraceRange tr("dyn_adjoint_forward");
     Ctx* c = C(p);
     if (c->d.mixed) return fail(DYN_ERR_UNSUPPORTED, "the adjoint runs on the FP64 form");
     if (c->d.logr) return fail(DYN_ERR_UNSUPPORTED, "the adjoint differentiates the linear-domain gathers only");
@@ -1320,6 +1325,7 @@ dyn_status dyn_adjoint_forward(void* p, const dyn_run_params* rp, dyn_step_resul
 
 dyn_status dyn_adjoint_backward(void* p, const dyn_adjoint_objective* obj, double* grad, dyn_adjoint_stats* stats) {
     if (!p || !obj || !grad) return fail(DYN_ERR_INVALID, "null argument");
+    TraceRange tr("dyn_adjoint_backward");
     Ctx* c = C(p);
     if (!c->adj_recorded || c->gen != c->adj_gen)
         return fail(DYN_ERR_STATE, "no recorded forward: call dyn_adjoint_forward (the history changed since)");
@@ -1406,6 +1412,7 @@ dyn_status dyn_adjoint_history_grad(void* p, dyn_state* g) {
 dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
     if (!p) return fail(DYN_ERR_INVALID, "null ctx");
     if (variant < 0 || variant > 2) return fail(DYN_ERR_INVALID, "unknown sparsify variant");
+    TraceRange tr("dyn_sparsify");
     Ctx* c = C(p);
     const size_t n = c->n;
     if (n_out) *n_out = n;

@@ -1040,6 +1040,7 @@ dyn_status dyn_batch_set_limits(void* p, int qi, double t_stop, long long max_st
 
 dyn_status dyn_batch_run(void* p, long long max_ticks, long long* ticks_out) {
     if (!p) return bfail(DYN_ERR_INVALID, "null argument");
+    TraceRange tr("dyn_batch_run");
     Batch* bt = BT(p);
     long long done = 0;
     dyn_status s = bt->read_plans();
@@ -1062,6 +1063,7 @@ dyn_status dyn_batch_run(void* p, long long max_ticks, long long* ticks_out) {
 
 dyn_status dyn_batch_enqueue(void* p, long long ticks) {
     if (!p || ticks < 0) return bfail(DYN_ERR_INVALID, "bad argument");
+    TraceRange tr("dyn_batch_enqueue");
     Batch* bt = BT(p);
     dyn_status s = bt->ensure_graph();
     if (s) return s;

@@ -3,11 +3,34 @@
 // the step-size limits and the model's f', f'' in the reference's host
 // expression order.
 #pragma once
+#include <nvtx3/nvToolsExt.h>
+#include <cstdlib>
 #include <string>
 #include <vector>
 #include "../../include/dyn.h"
 
 namespace dyn {
+
+// A named NVTX range over one host call or one step, for Nsight timelines and
+// `ncu --nvtx` filters.  Off unless the environment sets DYN_NVTX=1 (read once).
+inline bool trace_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("DYN_NVTX");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+struct TraceRange {
+    const bool on;
+    explicit TraceRange(const char* name) : on(trace_enabled()) {
+        if (on) nvtxRangePushA(name);
+    }
+    ~TraceRange() {
+        if (on) nvtxRangePop();
+    }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // rmax (config.hpp:33): stability radius of method m is RMAX[m-1] / specRad
 inline constexpr double RMAX[11] = {3, 13, 20, 80, 180, 320, 500, 720, 980, 1280, 1620};
