@@ -17,6 +17,10 @@ RK54GPU / SSPRK104GPU  Simulation.RK54 / SSPRK104 / SERK2
 sparsifyNscaleGPU      Simulation.sparsifyNscale (sparsify_utils.cu:199-290)
 rollbackState          Simulation.rollbackState (simulation_control.cpp:14)
 runSimulation loop     Simulation.run (simulation_runner.cpp:125-304)
+tailFitBlendCPU/GPU    Simulation.tail_fit (tail_fit.cpp:46-262)
+-R (log response)      Simulation(..., log_response=True) (index_vec.cpp:24-131)
+computeEnergyHistory   Simulation.energy_history (io_output.cu:61-122)
+saveCompressedData     Simulation.save_compressed (io_save_compressed.cpp:17-63)
 =====================  =====================================================
 
 Every numeric call goes to the CUDA library; nothing here computes on the
