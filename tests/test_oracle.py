@@ -172,3 +172,23 @@ def test_port_equals_reference_with_periodic_sparsify(oracle_built):
     for k in STATE_FIELDS:
         np.testing.assert_array_equal(getattr(s1, k), getattr(s2, k), err_msg=k)
     assert (O.Reference.lib().dynref_get_delta_t(), O.Reference.lib().dynref_get_method()) == port.controller()
+
+
+@pytest.mark.skipif(not O.Reference.available(), reason="reference sources not built here")
+@pytest.mark.parametrize("p,p2,lam,T0,Gamma", [(2, 3, 0.7, 2.0, 0.9), (4, 0, 0.5, 1e50, 0.5), (3, 5, 0.2, 0.8, 1.1)])
+def test_port_equals_reference_across_models(oracle_built, p, p2, lam, T0, Gamma):
+    """Other exponents (the generic f', f'', f''' by squaring, math_ops.cpp:7-37) and a
+    finite T0 (the f'(q0)/T0 terms of the RHS, r and the energy), 40 controller steps."""
+    g = O.Reference.grid(48, Tmax=20.0)
+    m = O.Model(p=p, p2=p2, lam=lam, T0=T0, Gamma=Gamma)
+    port = O.Port(g, m, search_mode=0, threads=1)
+    ref = O.Reference(g, m, threads=1)
+    ref.init_state()
+    port.init_state()
+    r1, r2 = ref.run(40), port.run(40)
+    for k in r1:
+        np.testing.assert_array_equal(r1[k], r2[k], err_msg=k)
+    s1, s2 = ref.get_state(), port.get_state()
+    for k in STATE_FIELDS:
+        np.testing.assert_array_equal(getattr(s1, k), getattr(s2, k), err_msg=k)
+    assert np.isfinite(s1.QK).all()
