@@ -192,3 +192,43 @@ def test_port_equals_reference_across_models(oracle_built, p, p2, lam, T0, Gamma
     for k in STATE_FIELDS:
         np.testing.assert_array_equal(getattr(s1, k), getattr(s2, k), err_msg=k)
     assert np.isfinite(s1.QK).all()
+
+
+def _cudahost_lib():
+    """sparsify_utils.cu's host-side sparsifyNscale (the reference's CUDA build), compiled
+    from the reference source on demand (nvcc; host code only runs)."""
+    import ctypes as C
+    import os
+    import subprocess
+    subprocess.run(["make", "-s", "-C", os.path.dirname(O.__file__), "cudahost"], check=True)
+    lib = C.CDLL(os.path.join(os.path.dirname(O.__file__), "_ref", "libdynref_cudahost.so"))
+    dp = C.POINTER(C.c_double)
+    lib.dynref_sparsify_cudahost.argtypes = [C.c_size_t, C.c_size_t] + [dp] * 8 + [C.c_double, C.POINTER(C.c_size_t)] \
+        + [dp] * 8
+    return lib
+
+
+@pytest.mark.skipif(not O.Reference.available(), reason="reference sources not built here")
+@pytest.mark.parametrize("L", SIZES)
+def test_cuda_host_sparsify_variant_equals_reference(oracle_built, L):
+    """Variant 1 ("cuda_host", sparsify_utils.cu:38-113: indicator over QK and QR only,
+    the delta_t_ratio rebuild before the resize) against the reference's own code."""
+    import ctypes as C
+    lib = _cudahost_lib()
+    g = load_golden(L)
+    st = state_from(g, "traj_final", O.State)
+    n = st.n
+    for thr in (float(g["spars_threshold"][0]), 10 * float(g["spars_threshold"][0])):
+        ins = [np.ascontiguousarray(getattr(st, k), dtype=np.float64) for k in STATE_FIELDS]
+        outs = [np.zeros_like(a) for a in ins]
+        k = C.c_size_t()
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        lib.dynref_sparsify_cudahost(n, L, *[ptr(a) for a in ins], thr, C.byref(k), *[ptr(a) for a in outs])
+        p = port_for(g)
+        p.set_state(st)
+        kk, _ = p.sparsify(thr, 1)
+        b = p.get_state()
+        assert kk == k.value < n
+        for name, o in zip(STATE_FIELDS, outs):
+            rows = k.value * (L if name in ("QK", "QR", "dQK", "dQR") else 1)
+            np.testing.assert_array_equal(getattr(b, name), o[:rows], err_msg=name)
