@@ -232,3 +232,32 @@ def test_cuda_host_sparsify_variant_equals_reference(oracle_built, L):
         for name, o in zip(STATE_FIELDS, outs):
             rows = k.value * (L if name in ("QK", "QR", "dQK", "dQR") else 1)
             np.testing.assert_array_equal(getattr(b, name), o[:rows], err_msg=name)
+
+
+@pytest.mark.parametrize("q,tol", [(2, 1e-13), (4, 1e-11), (6, 1e-10), (8, 1e-7)])
+def test_serk_coefficients_reproduce_the_stability_polynomial(oracle_built, q, tol):
+    """The reference's SERK2 exists on its GPU path only, so its coefficients are pinned
+    by what defines them (runge_kutta.cu:228-272): with s = 2q stages the combination
+    b_0 + sum_j sum_{i=1,2} b_{i+2(j-1)} T_i(1 + a z) T_2(1 + a z)^(j-1), a = q / s^2,
+    equals R(z) = T_s(w0 + w1 z) / T_s(w0), w0 = 1 + (19/20) / s^2,
+    w1 = T_s(w0) / (s U_{s-1}(w0)) — a degree-s polynomial identity, checked off the
+    s + 1 collocation points the coefficients were solved on."""
+    from numpy.polynomial import chebyshev as Ch
+    T = lambda n, x: Ch.chebval(x, [0] * n + [1])
+
+    def U(n, x):
+        u0, u1 = 1.0, 2.0 * x
+        for _ in range(n - 1):
+            u0, u1 = u1, 2.0 * x * u1 - u0
+        return u1 if n > 0 else 1.0
+
+    s = 2 * q
+    a, w0 = q / (s * s), 1.0 + (19.0 / 20.0) / (s * s)
+    w1 = T(s, w0) / (s * U(s - 1, w0))
+    b = O.Port.serk_coeffs(q)
+    z = np.linspace(-3.0, 3.0, 25)
+    basis = [T(0, 1 + a * z)] + [T(i, 1 + a * z) * T(2, 1 + a * z) ** (j - 1)
+                                 for j in range(1, q + 1) for i in (1, 2)]
+    comb = sum(bk * f for bk, f in zip(b, basis))
+    R = T(s, w0 + w1 * z) / T(s, w0)
+    assert np.max(np.abs(comb - R) / np.maximum(1.0, np.abs(R))) < tol
