@@ -261,3 +261,54 @@ def test_serk_coefficients_reproduce_the_stability_polynomial(oracle_built, q, t
     comb = sum(bk * f for bk, f in zip(b, basis))
     R = T(s, w0 + w1 * z) / T(s, w0)
     assert np.max(np.abs(comb - R) / np.maximum(1.0, np.abs(R))) < tol
+
+
+def _gpu_variant_numpy(st, L, thr):
+    """Variant 2 restated independently in numpy from the reference's CUDA code
+    (computeSparsifyFlags and sparsifyNscaleGPU, sparsify_utils.cu:154-290): flags of
+    the even nodes 2 <= i <= n-2, every other node kept; the QK and QR terms summed
+    alternately per column in index order; delta_t_ratio resized, then rebuilt from 2."""
+    t = st.t1grid
+    n = t.size
+    QK, QR, dQK, dQR = (np.asarray(getattr(st, k)).reshape(n, L) for k in ("QK", "QR", "dQK", "dQR"))
+    flags = np.ones(n, dtype=bool)
+    for i in range(2, n - 1, 2):
+        d1, d2, d3 = t[i - 1] - t[i - 2], t[i] - t[i - 2], t[i + 1] - t[i]
+        sc = d2 / 12.0
+        val = 0.0
+        for j in range(L):
+            val += abs(sc * (2.0 * (QK[i, j] - QK[i - 2, j]) - d2 * (dQK[i - 1, j] / d1 + dQK[i + 1, j] / d3)))
+            val += abs(sc * (2.0 * (QR[i, j] - QR[i - 2, j]) - d2 * (dQR[i - 1, j] / d1 + dQR[i + 1, j] / d3)))
+        flags[i] = val >= thr
+    keep = np.nonzero(flags)[0]
+    indsD = np.concatenate([[0], keep[:-1] + 1])
+    tfac = np.ones(keep.size)
+    for k in range(1, keep.size):
+        den = t[indsD[k]] - t[indsD[k] - 1]
+        tfac[k] = (t[keep[k]] - t[keep[k - 1]]) / den if den != 0.0 else 1.0
+    out = dict(t1grid=t[keep], QK=QK[keep].ravel(), QR=QR[keep].ravel(),
+               dQK=(dQK[indsD] * tfac[:, None]).ravel(), dQR=(dQR[indsD] * tfac[:, None]).ravel(),
+               rvec=np.asarray(st.rvec)[keep], drvec=np.asarray(st.drvec)[indsD] * tfac)
+    dtr = np.array(st.dtr[:keep.size], dtype=np.float64)
+    tk = out["t1grid"]
+    for k in range(2, keep.size):
+        dtr[k] = (tk[k] - tk[k - 1]) / (tk[k - 1] - tk[k - 2])
+    out["dtr"] = dtr
+    return keep, out
+
+
+@pytest.mark.parametrize("L", SIZES)
+def test_gpu_sparsify_variant_against_an_independent_restatement(oracle_built, L):
+    """The oracle's variant 2 (what the CUDA path is held to) equals a second,
+    independent restatement of the reference's CUDA sparsify, bit for bit."""
+    g = load_golden(L)
+    st = state_from(g, "traj_final", O.State)
+    for thr in (float(g["spars_threshold"][0]), 4 * float(g["spars_threshold"][0])):
+        keep, want = _gpu_variant_numpy(st, L, thr)
+        p = port_for(g)
+        p.set_state(st)
+        k, _ = p.sparsify(thr, 2)
+        b = p.get_state()
+        assert k == keep.size < st.n
+        for name, a in want.items():
+            np.testing.assert_array_equal(getattr(b, name), a, err_msg=name)
