@@ -4,7 +4,7 @@ Bit-exact where the reference computes integers or where the CUDA kernel
 uses the reference's operation order (materialized interpolation, QKRstep,
 r, dr, energy, positions, sparsify keep lists); within stated tolerances
 where the fused kernels reassociate sums (fused RHS: 1e-12 relative; one RK
-step: 1e-12; fixed-schedule trajectories: 1e-10, the spec bar for the
+step: 1e-12; fixed-schedule trajectories: 1e-10, the parity bar for the
 plain FP64 form).
 """
 import numpy as np
