@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-mixed", dest="mixed", action="store_false", help="skip the single-quench mixed measurement")
     ap.add_argument("--quenches", type=int, default=64)
     ap.add_argument("--tune", action="store_true", help="autotune the batched gather tile before timing")
-    ap.add_argument("--config4-setup", type=int, default=1000,
+    ap.add_argument("--mixed-length-setup", type=int, default=1000,
                     help="untimed steps of every quench of the mixed-L batch before its timed ticks (0: skip it)")
     ap.add_argument("--adjoint-steps", type=int, default=5000, help="FP64 steps of the adjoint measurement (0: skip)")
     ap.add_argument("--no-df", dest="df", action="store_false", help="skip the batched (hi, lo) form")
@@ -341,14 +341,14 @@ def _batch_df(D, torch, args, grid, dev, stream):
     return out
 
 
-def _config4(D, torch, args, dev, stream):
+def _mixed_length_batch(D, torch, args, dev, stream):
     """The mixed-L batch: 64 quenches, temperatures uniform on [0.4, 1.0], lambda cycling
     0.3/0.5/0.7, grid length from {256, 512, 1024} and stopping time log-uniform on [1e4, 1e7]
-    drawn from mt19937_64 (fixed seed), mixed precision.  Every quench takes `config4_setup`
+    drawn from mt19937_64 (fixed seed), mixed precision.  Every quench takes `mixed_length_setup`
     steps untimed from t=0, then `steps` ticks are timed; value = RK steps completed / time."""
-    from dynamite_gb300.batch import config4_quenches
-    cap = args.config4_setup + args.steps + 64
-    lengths, qs = config4_quenches(n=args.quenches, capacity=cap, max_steps=args.config4_setup)
+    from dynamite_gb300.batch import mixed_length_quenches
+    cap = args.mixed_length_setup + args.steps + 64
+    lengths, qs = mixed_length_quenches(n=args.quenches, capacity=cap, max_steps=args.mixed_length_setup)
     grids = [D.grid.generate(L) for L in lengths]
     bt = D.Batch(grids, qs, ticks_per_launch=32, device=dev, stream=stream.cuda_stream)
     bt.run(10 ** 9)
@@ -371,7 +371,7 @@ def _config4(D, torch, args, dev, stream):
            "ms_per_tick": 1e3 * t / args.steps, "quenches_per_L": per_L,
            "t_stop_range": [min(q.t_stop for q in qs), max(q.t_stop for q in qs)],
            "t_reached_range": [min(i["t"] for i in infos), max(i["t"] for i in infos)],
-           "setup_steps": args.config4_setup,
+           "setup_steps": args.mixed_length_setup,
            "note": "timed window of the job after the untimed setup; no quench reaches its stopping time "
                    "inside the window"}
     bt.close()
@@ -505,7 +505,7 @@ def run_ours(args):
     if rank != 0:
         return
     batch_df = _batch_df(D, torch, args, grid, dev, stream) if args.df else None
-    config4 = _config4(D, torch, args, dev, stream) if args.config4_setup > 0 else None
+    mixed_length = _mixed_length_batch(D, torch, args, dev, stream) if args.mixed_length_setup > 0 else None
     adjoint = _adjoint(D, torch, args, dev) if args.adjoint_steps > 0 else None
     # ---- roofline of the dominant kernel: the batched gather, timed live on its stream
     ms_gather = bt.profile(reps=10)
@@ -544,7 +544,7 @@ def run_ours(args):
         "mixed_single": mixed,
         "batched_mixed_df": None if batch_df is None else dict(batch_df, speedup_vs_fp64=batch_df["value"] / fp64["value"],
                                                                  note="the (hi, lo) form: ~100x smaller long-run error"),
-        "config4_mixed_L": config4,
+        "mixed_length_batch": mixed_length,
         "adjoint": adjoint,
         "e2e": {"value": e2e_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h_tick, "note": "per tick; dyn_batch_run of 32 ticks + newest rows"},

@@ -14,7 +14,7 @@ sparsify (simulation_runner.cpp:148-237) after each loop that is a multiple
 of it: it pauses at that step's end and the host compacts its history between
 graph replays.
 
-`config4_quenches` draws the 64-quench workload (temperatures on [0.4, 1.0],
+`mixed_length_quenches` draws the 64-quench workload (temperatures on [0.4, 1.0],
 lambda in {0.3, 0.5, 0.7}, grid length from {256, 512, 1024}, stopping times
 log-uniform on [1e4, 1e7]) from `mt19937_64` with a fixed seed.
 """
@@ -207,7 +207,7 @@ class MT19937_64:
         return (self() >> 11) * (1.0 / 9007199254740992.0)
 
 
-def config4_quenches(n: int = 64, seed: int = 20261203, lengths=(256, 512, 1024), capacity: int = 4096,
+def mixed_length_quenches(n: int = 64, seed: int = 20261203, lengths=(256, 512, 1024), capacity: int = 4096,
                      max_steps: int = 0):
     """The batched-quench workload: quench b has temperature Gamma_b = 0.4 + 0.6 b/(n-1),
     lambda cycling through {0.3, 0.5, 0.7}, grid length lengths[x % 3] and stopping time

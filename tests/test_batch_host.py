@@ -1,7 +1,7 @@
 """Host-side logic of the batched quenches (no GPU): the seeded workload draw."""
 import math
 
-from dynamite_gb300.batch import MT19937_64, config4_quenches
+from dynamite_gb300.batch import MT19937_64, mixed_length_quenches
 
 
 def test_mt19937_64_matches_the_standard():
@@ -12,15 +12,15 @@ def test_mt19937_64_matches_the_standard():
     assert r() == 9981545732273789042
 
 
-def test_config4_workload():
-    lengths, qs = config4_quenches()
+def test_mixed_length_workload():
+    lengths, qs = mixed_length_quenches()
     assert lengths == [256, 512, 1024] and len(qs) == 64
     assert {q.lam for q in qs} == {0.3, 0.5, 0.7}
     assert qs[0].Gamma == 0.4 and abs(qs[-1].Gamma - 1.0) < 1e-15
     assert all(1e4 <= q.t_stop < 1e7 for q in qs)
     assert {q.grid for q in qs} == {0, 1, 2}
     # the draw is deterministic
-    _, again = config4_quenches()
+    _, again = mixed_length_quenches()
     assert [(q.grid, q.t_stop) for q in qs] == [(q.grid, q.t_stop) for q in again]
     # log-uniform: the mean of log10(t_stop) sits near 5.5
     assert abs(sum(math.log10(q.t_stop) for q in qs) / 64 - 5.5) < 0.5
