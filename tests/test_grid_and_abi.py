@@ -194,3 +194,39 @@ def test_batch_and_adjoint_arguments_rejected_without_touching_the_gpu(product_b
     assert L.dyn_adjoint_forward(None, None, None) == -1
     assert L.dyn_adjoint_backward(None, None, None, None) == -1
     assert L.dyn_batch_run(None, 1, None) == -1
+
+
+STRUCTS = [("Config", "dyn_config"), ("Tables", "dyn_tables"), ("StateC", "dyn_state"),
+           ("Controller", "dyn_controller"), ("StepResult", "dyn_step_result"), ("RunParams", "dyn_run_params"),
+           ("TailInfo", "dyn_tail_info"), ("NoAllocRHS", "dyn_noalloc_rhs"), ("BatchGrid", "dyn_batch_grid"),
+           ("BatchQuench", "dyn_batch_quench"), ("BatchConfig", "dyn_batch_config"), ("BatchInfo", "dyn_batch_info"),
+           ("AdjointObjective", "dyn_adjoint_objective"), ("AdjointStats", "dyn_adjoint_stats")]
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror of an include/dyn.h struct has the C compiler's size and field
+    offsets (a field added on one side only would shift the rest silently)."""
+    import shutil
+    import subprocess
+    from dynamite_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    c_name = {"lam": "lambda"}  # Python keyword
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "dyn.h"', "int main(void) {"]
+    for py, c in STRUCTS:
+        lines.append(f'printf("{py} size %zu\\n", sizeof({c}));')
+        for name, _ in getattr(_lib, py)._fields_:
+            lines.append(f'printf("{py} {name} %zu\\n", offsetof({c}, {c_name.get(name, name)}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                                 text=True).stdout.splitlines())
+    for py, _ in STRUCTS:
+        S = getattr(_lib, py)
+        assert int(got[f"{py} size"]) == C.sizeof(S), py
+        for name, _ in S._fields_:
+            assert int(got[f"{py} {name}"]) == getattr(S, name).offset, (py, name)
