@@ -312,3 +312,17 @@ def test_gpu_sparsify_variant_against_an_independent_restatement(oracle_built, L
         assert k == keep.size < st.n
         for name, a in want.items():
             np.testing.assert_array_equal(getattr(b, name), a, err_msg=name)
+
+
+@pytest.mark.parametrize("L", SIZES)
+def test_equal_time_values_stay_one(oracle_built, L):
+    """The reference does not enforce C(t,t) = 1 (the spherical constraint) or R(t,t) = 1;
+    r(t) is what keeps them (time_steps.cpp:83-92).  Along a 120-step controller run
+    the theta = 1 column of every history row stays 1."""
+    g = load_golden(L)
+    p = port_for(g)
+    p.init_state()
+    p.run(120)
+    st = p.get_state()
+    assert np.max(np.abs(st.QK.reshape(-1, L)[:, -1] - 1.0)) < 1e-12
+    assert np.max(np.abs(st.QR.reshape(-1, L)[:, -1] - 1.0)) < 1e-12
