@@ -316,9 +316,10 @@ def test_gpu_sparsify_variant_against_an_independent_restatement(oracle_built, L
 
 @pytest.mark.parametrize("L", SIZES)
 def test_equal_time_values_stay_one(oracle_built, L):
-    """The reference does not enforce C(t,t) = 1 (the spherical constraint) or R(t,t) = 1;
-    r(t) is what keeps them (time_steps.cpp:83-92).  Along a 120-step controller run
-    the theta = 1 column of every history row stays 1."""
+    """The reference does not enforce C(t,t) = 1 (the spherical constraint) or R(t,t) = 1
+    explicitly: the Lagrange multiplier r(t) (time_steps.cpp:83-92) keeps the first and
+    the equations of motion the second.  Along a 120-step controller run the theta = 1
+    column of every history row stays 1."""
     g = load_golden(L)
     p = port_for(g)
     p.init_state()
