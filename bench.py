@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-mixed", dest="mixed", action="store_false", help="skip the single-quench mixed measurement")
     ap.add_argument("--quenches", type=int, default=64)
-    ap.add_argument("--tune", action="store_true", help="autotune the batched gather tile before timing")
+    ap.add_argument("--no-tune", dest="tune", action="store_false",
+                    help="skip the autotuner (dyn_batch_tune) that picks the batched gather tile before timing")
     ap.add_argument("--mixed-length-setup", type=int, default=1000,
                     help="untimed steps of every quench of the mixed-L batch before its timed ticks (0: skip it)")
     ap.add_argument("--adjoint-steps", type=int, default=5000, help="FP64 steps of the adjoint measurement (0: skip)")
@@ -167,34 +168,46 @@ def cpu_port_steps_per_s(st_dict, grid, seconds: float, max_steps: int):
     return k / el, k, el
 
 
+def _reference_grid(L: int):
+    """The L x L poly-9 tables for the CPU arm without loading this repository's library
+    into the timing process: the reference generator's own tables where the reference was
+    built (oracle/_ref), else the same tables written by the native generator in a child
+    process."""
+    import oracle as O
+    path = O.grid_cache_path(L)
+    src = "the reference generator (oracle/_ref)"
+    if not os.path.exists(path):
+        code = ("import sys; sys.path.insert(0, %r); import oracle, dynamite_gb300 as D; "
+                "oracle.save_grid(D.grid.generate(%d), %r)" % (ROOT, L, path))
+        subprocess.run([sys.executable, "-c", code], check=True)
+        src = "this repository's generator, run in a child process"
+    return O.load_grid(path), src
+
+
 def run_reference(args):
-    """The reference CPU path on the host cores (oracle/_ref where the reference
-    compiled here, otherwise the C restatement), same workload."""
+    """The reference CPU path on the host cores (oracle/_ref where the reference compiled
+    here, otherwise the C restatement pinned to it), on our arm's workload: the same grid,
+    model, setup, warm-up and timed steps (each a bounded sample: at most `cpu_seconds`)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import oracle as O
-    import dynamite_gb300 as D
-    grid = D.grid.generate(args.L)
-    og = O.Grid(grid.L, grid.theta, grid.phi1, grid.phi2, grid.integ, grid.indsA1, grid.wA1, grid.indsA2,
-                grid.wA2, grid.indsB2, grid.wB2)
+    grid, grid_src = _reference_grid(args.L)
     kind, impl = "port", None
     if os.path.exists(O.REF_FAST_LIB):
         try:
             O.Reference.lib(fast=True)
-            impl = O.Reference(og, O.Model(**model_kw()), threads=os.cpu_count())
+            impl = O.Reference(grid, O.Model(**model_kw()), threads=os.cpu_count())
             kind = "reference"
         except OSError:
             impl = None
     if impl is None:
         O.build(reference=False)
-        impl = O.Port(og, O.Model(**model_kw()), search_mode=0, threads=0)
+        impl = O.Port(grid, O.Model(**model_kw()), search_mode=0, threads=0)
     cores = os.cpu_count()
     impl.init_state()
-    setup = min(args.setup, 300)
-    impl.run(setup)
-    for _ in range(min(args.warmup, 3)):
-        impl.run(1)
+    impl.run(args.setup)
+    impl.run(args.warmup)
     t0 = time.perf_counter()
     k = 0
     while k < args.steps and (time.perf_counter() - t0) < args.cpu_seconds:
@@ -204,17 +217,26 @@ def run_reference(args):
     v = k / el
     out = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
-        "warmup": min(args.warmup, 3), "ms_per_step": 1e3 * el / k, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / k, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.quenches} quenches at L={args.L} (mixed p-spin -p 3 -q 4, T on [0.4, 1.0], "
-                               f"lam 0.3/0.5/0.7, poly-9 grid Tmax 1e5), run one after another on the host "
-                               f"cores; sampled on the lam=0.5, T=0.6 quench", "L": args.L, "quenches": args.quenches},
+        "config": _config(args),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": f"{k} controller iterations of one quench after {setup} setup steps from t=0 "
-                                   f"(per-step cost does not depend on T or lam)"},
+                         "sample": f"{k} controller iterations of the lam=0.5, T=0.6 quench after {args.setup} setup "
+                                   f"and {args.warmup} warm-up steps from t=0 (per-step cost does not depend on T or "
+                                   f"lam); tables from {grid_src}"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
+
+
+def _config(args):
+    """The workload both arms name: the batched quenches at L (the reference runs them one
+    after another; its per-step cost is that of any one of them)."""
+    return {"workload": f"{args.quenches} quenches at L={args.L}: reference model -p 3 -q 4 -l 0.5 "
+                        f"(f = (1-lam) q^3 + lam q^4, Gamma = bath T literally, no 1/2 rescaling), "
+                        f"T uniform on [0.4, 1.0], lam cycling 0.3/0.5/0.7, poly-9 grid Tmax 1e5 s=5, "
+                        f"after {args.setup} steps of each",
+            "L": args.L, "quenches": args.quenches, "setup_steps": args.setup}
 
 
 def replica_barrier(world: int) -> None:
@@ -523,40 +545,46 @@ def run_ours(args):
         cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                "sample": f"{k} controller iterations ({el:.1f} s) of one quench (lam=0.5, T=0.6) from the FP64 "
                          f"run's state after {args.setup} steps; per-step cost does not depend on T or lam"}
+    r3 = lambda x: None if x is None else float(f"{x:.4g}")
+    dram_gbs = None if traffic is None else traffic * B / 64 / (ms_gather * 1e-3) / 1e9
+    cfg = _config(args)
+    cfg.update({"step": "one tick = one RK stage of every quench", "rk_steps_timed": rk_steps_all,
+                "history_rows": [min(hist), max(hist)], "l2": "inputs > L2 (histories + tables > 1 GB)",
+                "tile": tune or {"threads": 128, "targets": 1}, "precision": "mixed: FP32 gathers/convolutions "
+                "with compensated sums; FP64 r(t), t, C(t,t), error norm",
+                "parallelism": "replicas" if world > 1 else "single GPU"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_batch / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": f"{B} quenches at L={L} (mixed p-spin -p 3 -q 4, T uniform on [0.4, 1.0], "
-                               f"lam cycling 0.3/0.5/0.7, poly-9 grid Tmax 1e5), mixed precision, batched; "
-                               f"timed after {args.setup} steps of every quench",
-                   "L": L, "quenches": B, "step": "one tick = one RK stage of every quench",
-                   "rk_steps_timed": rk_steps_all, "history_rows": [min(hist), max(hist)],
-                   "ticks_before_timed": ticks_before,
-                   "l2": "inputs larger than L2 (histories + tables of all quenches > 1 GB)",
-                   "tile": tune or {"threads": 128, "targets": 1},
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "speedup_vs_fp64": value / fp64["value"],
-        "fp64": dict(fp64, roofline={"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak,
-                                     "unit": "GFLOP/s", "frac": fp64_achieved / fp64_peak,
-                                     "flop_per_launch": fp64_flop, "kernel": "k_main (FP64 fused gather)",
-                                     "peak_source": "measured (dyn_probe_fp64, same run)"}),
-        "mixed_single": mixed,
-        "batched_mixed_df": None if batch_df is None else dict(batch_df, speedup_vs_fp64=batch_df["value"] / fp64["value"],
-                                                                 note="the (hi, lo) form: ~100x smaller long-run error"),
-        "mixed_length_batch": mixed_length,
-        "adjoint": adjoint,
+        # the comparison points first, short: the plain FP64 form of one quench on the same grid
+        "fp64": {"value": r3(fp64["value"]), "ms_per_step": r3(fp64["ms_per_step"]),
+                 "k_main_ms": r3(fp64["stage_ms"]["main"]), "k_main_frac_fp64": r3(fp64_achieved / fp64_peak),
+                 "fp64_peak_gflops": r3(fp64_peak)},
+        "speedup_vs_fp64": r3(value / fp64["value"]),
+        "mixed_df": None if batch_df is None else {"value": r3(batch_df["value"]),
+                                                   "speedup_vs_fp64": r3(batch_df["value"] / fp64["value"])},
+        "mixed_single": None if mixed is None else r3(mixed["value"]),
+        "adjoint": None if adjoint is None else {
+            "bwd_fwd": r3(adjoint["bwd_fwd_ratio"]), "steps": adjoint["steps"],
+            "max_rel_err_vs_fd": r3(max(v["rel_err"] for v in adjoint["all_gradients"].values())),
+            "peak_gb": r3(adjoint["peak_device_bytes"] / 1e9), "recompute_mismatch": adjoint["recompute_mismatch"]},
+        "mixed_L_batch": None if mixed_length is None else {
+            "value": r3(mixed_length["value"]), "per_L": mixed_length["quenches_per_L"],
+            "t_reached": [r3(x) for x in mixed_length["t_reached_range"]]},
         "e2e": {"value": e2e_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": d2h_tick, "note": "per tick; dyn_batch_run of 32 ticks + newest rows"},
+                "d2h_bytes_per_step": d2h_tick,
+                "note": "per tick, through dyn_batch_run (32-tick graph replays) + each quench's newest row read "
+                        "back; the histories stay resident in HBM by design, so no per-step H2D input exists"},
         "gpu_launches": int(2 * args.steps),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None if traffic is None else traffic * B / 64,
-                     "kernel": "k_batch_gather (all quenches, one stage)", "ms_per_launch": ms_gather,
-                     "alg_bytes_per_launch": alg_bytes, "peak_source": src,
-                     "note": "tables counted once per launch (shared by the quenches on the grid); the kernel "
-                             "is L1/issue-bound, not HBM-bound (profiles/k_batch_gather_L512.txt)"},
+                     "frac_dram": None if dram_gbs is None else r3(dram_gbs / peaks["hbm_gbs"]),
+                     "kernel": "k_batch_gather", "ms_per_launch": r3(ms_gather), "peak_source": src,
+                     "note": "alg bytes = tables once + FP32 history rows per quench; L1/issue-bound"},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "config": cfg,
     }
     bt.close()
     print(json.dumps(line))

@@ -132,7 +132,15 @@ _lib = None
 
 
 class DynError(RuntimeError):
-    pass
+    """A dyn_status other than DYN_OK; `status` holds the code."""
+
+    def __init__(self, msg: str, status: int = 0):
+        super().__init__(msg)
+        self.status = status
+
+
+DYN_ERR_INVALID, DYN_ERR_CUDA, DYN_ERR_NOMEM, DYN_ERR_STATE, DYN_ERR_UNSUPPORTED, DYN_ERR_NONFINITE = (
+    -1, -2, -3, -4, -5, -6)
 
 
 def lib():
@@ -150,6 +158,7 @@ def lib():
             "dyn_tail_fit_reset": ([vp], C.c_int),
             "dyn_last_error": ([], C.c_char_p),
             "dyn_ctx_create": ([C.POINTER(Config), C.POINTER(Tables), C.POINTER(vp)], C.c_int),
+            "dyn_check_tables": ([C.c_size_t, C.c_size_t, C.POINTER(Tables)], C.c_int),
             "dyn_ctx_destroy": ([vp], C.c_int),
             "dyn_sync": ([vp], C.c_int),
             "dyn_state_init": ([vp, C.c_double], C.c_int),
@@ -210,7 +219,7 @@ def lib():
 def check(status: int, what: str = "") -> None:
     if status != DYN_OK:
         msg = lib().dyn_last_error().decode(errors="replace")
-        raise DynError(f"{what} failed (status {status}): {msg}")
+        raise DynError(f"{what} failed (status {status}): {msg}", status)
 
 
 def ptr(a):

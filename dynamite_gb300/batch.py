@@ -29,7 +29,7 @@ from . import _lib
 from .grid import Grid
 from .simulation import SEARCH, SPARSIFY, State
 
-STATUS = {0: "running", 1: "done", 2: "max_steps", 3: "full", 4: "sparsify"}
+STATUS = {0: "running", 1: "done", 2: "max_steps", 3: "full", 4: "sparsify", 5: "failed"}
 
 
 @dataclass

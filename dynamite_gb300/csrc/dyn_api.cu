@@ -217,6 +217,14 @@ struct Ctx {
         return DYN_OK;
     }
 
+    // After the history shrank or was replaced (old length n_old): the FP32 mirror
+    // rows [n, n_old + 1) leave the history and are zeroed (clear_mirror_rows)
+    dyn_status clear_tail(size_t n_old) {
+        if (!d.mixed) return DYN_OK;
+        CK(clear_mirror_rows(d, n, std::min(std::max(n_old, n) + 1, cap), st));
+        return DYN_OK;
+    }
+
     // With theta[L-1] == phi2[L*L-1] == 1 (checked at creation) the largest
     // position of both searches is the last row exactly, so the reference's
     // clamps ceil(max posB1x) - 1 (interpolation_core.cpp:58-67) and
@@ -535,6 +543,22 @@ bool check_tables(size_t L, size_t m, const dyn_tables* tb, std::vector<int> i32
     for (size_t e = 0; e < L2; ++e)
         if (!(tb->phi2[e] >= 0.0 && tb->phi2[e] <= 1.0)) { why = "phi2 outside [0, 1]"; return false; }
     if (tb->phi2[L2 - 1] != 1.0) { why = "phi2 must end at 1"; return false; }
+    for (size_t i = 0; i < L; ++i)
+        if (!std::isfinite(tb->integ[i])) { why = "int.dat holds a non-finite weight"; return false; }
+    const double* w[3] = {tb->weightsA1y, tb->weightsA2y, tb->weightsB2y};
+    for (int k = 0; k < 3; ++k)
+        for (size_t e = 0; e < L2 * m; ++e)
+            if (!std::isfinite(w[k][e])) { why = "a stencil weight is not finite"; return false; }
+    return true;
+}
+
+// The model parameters the kernels can evaluate: f'(q), f''(q), f'''(q) with
+// integer exponents, 1/T0, and a finite bath temperature.
+bool check_model(int p_, int p2_, double lambda, double T0, double Gamma, std::string& why) {
+    if (p_ < 0 || p2_ < 0 || p_ > 64 || p2_ > 64) { why = "exponents p, p2 must be in [0, 64]"; return false; }
+    if (!std::isfinite(lambda)) { why = "lambda must be finite"; return false; }
+    if (!(T0 > 0.0)) { why = "T0 must be positive (1e50 for an infinite-temperature start)"; return false; }
+    if (!std::isfinite(Gamma)) { why = "Gamma must be finite"; return false; }
     return true;
 }
 
@@ -693,6 +717,16 @@ extern "C" {
 int dyn_abi_version(void) { return DYN_ABI_VERSION; }
 const char* dyn_last_error(void) { return g_err.c_str(); }
 
+dyn_status dyn_check_tables(size_t len, size_t depth, const dyn_tables* tb) {
+    if (!tb) return fail(DYN_ERR_INVALID, "null argument");
+    if (len < 4 || len > 4096 || depth < 2 || depth > len)
+        return fail(DYN_ERR_INVALID, "len must be in [4, 4096] and 2 <= depth <= len");
+    std::vector<int> i32[3];
+    std::string why;
+    if (!check_tables(len, depth, tb, i32, why)) return fail(DYN_ERR_INVALID, why);
+    return DYN_OK;
+}
+
 dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** out) {
     if (!cfg || !tb || !out) return fail(DYN_ERR_INVALID, "null argument");
     *out = nullptr;
@@ -707,6 +741,7 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
     std::vector<int> i32[3];
     {
         std::string why;
+        if (!check_model(cfg->p, cfg->p2, cfg->lambda, cfg->T0, cfg->Gamma, why)) return fail(DYN_ERR_INVALID, why);
         if (!check_tables(L, m, tb, i32, why)) return fail(DYN_ERR_INVALID, why);
     }
 
@@ -828,6 +863,7 @@ dyn_status dyn_state_init(void* p, double delta_t) {
     if (!p) return fail(DYN_ERR_INVALID, "null ctx");
     Ctx* c = C(p);
     const int L = c->L;
+    const size_t n_old = c->n;
     c->n = 1;
     c->gen++;
     c->t1.assign(1, 0.0);
@@ -841,6 +877,7 @@ dyn_status dyn_state_init(void* p, double delta_t) {
     if (s) return s;
     CK(launch_rstep_exact(c->d, 1, c->d.drvec, c->st));
     if ((s = c->mirror_all())) return s;
+    if ((s = c->clear_tail(n_old))) return s;
     c->ctl.delta_t = delta_t > 0 ? delta_t : c->cfg.delta_t_min;
     c->ctl.loop = 0;
     c->last_rollback_loop = -1000;
@@ -860,11 +897,19 @@ dyn_status dyn_state_upload(void* p, const dyn_state* stt) {
     if (!stt->t1grid || !stt->delta_t_ratio || !stt->QK || !stt->QR || !stt->dQK || !stt->dQR || !stt->rvec || !stt->drvec)
         return fail(DYN_ERR_INVALID, "missing state array");
     for (size_t k = 0; k < n; ++k) {
-        if (!(stt->t1grid[k] >= 0.0)) return fail(DYN_ERR_INVALID, "t1grid must be non-negative");
+        if (!(stt->t1grid[k] >= 0.0) || !std::isfinite(stt->t1grid[k]))
+            return fail(DYN_ERR_INVALID, "t1grid must be finite and non-negative");
         if (k && !(stt->t1grid[k] >= stt->t1grid[k - 1])) return fail(DYN_ERR_INVALID, "t1grid must be non-decreasing");
+        if (!std::isfinite(stt->delta_t_ratio[k]) || !std::isfinite(stt->rvec[k]) || !std::isfinite(stt->drvec[k]))
+            return fail(DYN_ERR_INVALID, "delta_t_ratio, rvec and drvec must be finite");
     }
+    for (size_t e = 0; e < n * L; ++e)
+        if (!std::isfinite(stt->QK[e]) || !std::isfinite(stt->QR[e]) || !std::isfinite(stt->dQK[e]) ||
+            !std::isfinite(stt->dQR[e]))
+            return fail(DYN_ERR_INVALID, "QK, QR, dQK and dQR must be finite");
     c->drop_graphs();
     c->gen++;
+    const size_t n_old = c->n;
     c->n = 0;
     dyn_status s = c->ensure_rows(n + 1);
     if (s) return s;
@@ -881,6 +926,7 @@ dyn_status dyn_state_upload(void* p, const dyn_state* stt) {
     c->t1.assign(stt->t1grid, stt->t1grid + n);
     c->dtr.assign(stt->delta_t_ratio, stt->delta_t_ratio + n);
     if ((s = c->mirror_all())) return s;
+    if ((s = c->clear_tail(n_old))) return s;
     if ((s = c->upload_times())) return s;
     if ((s = c->pos_init())) return s;
     CK(cudaStreamSynchronize(c->st));
@@ -1115,6 +1161,8 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
     Ctx* c = C(p);
     dyn_controller& k = c->ctl;
     const double dmax = c->cfg.delta_max, dmin = c->cfg.delta_t_min;
+    if (!rp->dt_schedule && (k.method < 1 || !(k.delta_t > 0.0)))
+        return fail(DYN_ERR_STATE, "no step size or method: call dyn_controller_set after dyn_state_upload");
     dyn_step_result r{};
     for (int it = 0; it < rp->nsteps; ++it) {
         if (rp->tmax > 0 && c->t1[c->n - 1] >= rp->tmax) break;
@@ -1129,6 +1177,16 @@ dyn_status dyn_run(void* p, const dyn_run_params* rp, dyn_step_result* last) {
         k.delta_old = k.delta;
         dyn_status s = c->step(k.method, k.delta_t, &r);
         if (s) return s;
+        if (!std::isfinite(r.delta)) {
+            // the state holds non-finite values: stop before the controller acts on them
+            if (rp->out_delta) rp->out_delta[it] = r.delta;
+            if (rp->out_t) rp->out_t[it] = t;
+            if (rp->out_energy) rp->out_energy[it] = r.energy;
+            if (rp->out_qk0) rp->out_qk0[it] = r.qk0;
+            if (rp->out_r) rp->out_r[it] = r.r;
+            if (last) *last = r;
+            return fail(DYN_ERR_NONFINITE, "dyn_run: non-finite error estimate at iteration " + std::to_string(it));
+        }
         k.delta = r.delta;
         if (rp->tail_fit) {  // simulation_runner.cpp:135-141
             if ((s = tail_fit(c, c->last_rollback_loop))) return s;
@@ -1189,9 +1247,10 @@ dyn_status dyn_rollback(void* p, int nrows) {
     if (!p) return fail(DYN_ERR_INVALID, "null ctx");
     Ctx* c = C(p);
     if (nrows < 0 || (size_t)nrows >= c->n - 1) return fail(DYN_ERR_INVALID, "cannot roll back that many rows");
-    const size_t target = c->n - nrows;
+    const size_t target = c->n - nrows, n_old = c->n;
     c->n = target;
     c->gen++;
+    if (dyn_status cs = c->clear_tail(n_old)) return cs;
     c->t1.resize(target);
     c->dtr.resize(target);
     c->ctl.delta_t = c->t1[target - 1] - c->t1[target - 2];
@@ -1449,9 +1508,11 @@ dyn_status dyn_sparsify(void* p, double threshold, int variant, size_t* n_out) {
     c->drop_graphs();
     c->t1 = t1n;
     c->dtr = dtrn;
+    const size_t n_old = c->n;
     c->n = k;
     c->gen++;
     if ((s = c->mirror_all())) return s;
+    if ((s = c->clear_tail(n_old))) return s;
     if ((s = c->upload_times())) return s;
     if ((s = c->pos_init())) return s;
     CK(cudaStreamSynchronize(c->st));

@@ -76,6 +76,7 @@ struct Work {
 // runge_kutta.cpp:182-252 / runge_kutta.cu:397-487 time arithmetic) with the
 // host's operation order: every product and sum rounded as written.
 __device__ void begin_step(const Quench& q, Plan& pl, const TabDev& tb) {
+    if (pl.status == DYN_QUENCH_FAILED) return;  // only a new state (dyn_batch_upload) restarts it
     if (q.t_stop > 0.0 && pl.T_last >= q.t_stop) { pl.status = DYN_QUENCH_DONE; return; }
     if (q.max_steps > 0 && pl.steps >= q.max_steps) { pl.status = DYN_QUENCH_MAXSTEPS; return; }
     if (pl.n + 1 > q.cap) { pl.status = DYN_QUENCH_FULL; return; }
@@ -331,6 +332,11 @@ __global__ void __launch_bounds__(EPI_T) k_batch_epi(const Quench* __restrict__ 
         return;
     }
     finish_step(q, pl, sp);
+    if (!isfinite(pl.delta)) {
+        // non-finite values in the state (dyn_run's DYN_ERR_NONFINITE): stop this quench
+        pl.status = DYN_QUENCH_FAILED;
+        return;
+    }
     if (sparsify_due(q, pl)) {
         // the host compacts the history, then k_batch_resume adapts and plans
         pl.status = DYN_QUENCH_SPARSIFY;
@@ -573,7 +579,8 @@ struct Batch {
             launch_mirror_rows(q.c.KR, q.c.KRf, k * L, st) == cudaSuccess &&
             launch_mirror_rows(q.c.dKR, q.c.dKRf, k * L, st) == cudaSuccess &&
             (!q.c.KRl || launch_mirror_lo(q.c.KR, q.c.KRl, k * L, st) == cudaSuccess) &&
-            launch_time_f32(q.c.t1grid, q.c.dtr, (int)k, q.c.inv_len_f, q.c.inv_dtr_f, st) == cudaSuccess;
+            launch_time_f32(q.c.t1grid, q.c.dtr, (int)k, q.c.inv_len_f, q.c.inv_dtr_f, st) == cudaSuccess &&
+            clear_mirror_rows(q.c, k, std::min((size_t)pl.n + 1, (size_t)q.cap), st) == cudaSuccess;
         e = cudaStreamSynchronize(st);  // the host vectors above are sources of the copies
         release();
         if (!ok || e != cudaSuccess) return bfail(DYN_ERR_CUDA, "batch sparsify: " + std::string(cudaGetErrorString(cudaGetLastError())));
@@ -710,6 +717,15 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         if (q.p < 2 || q.p2 < 0 || q.p2 == 1) return bfail(DYN_ERR_INVALID, "quench exponents: p >= 2, p2 = 0 or >= 2");
         if (!(q.T0 > 0) || !(q.delta_t_min > 0) || !(q.delta_max > 0)) return bfail(DYN_ERR_INVALID, "T0, delta_t_min and delta_max must be positive");
         if (q.capacity != 0 && q.capacity < 2) return bfail(DYN_ERR_INVALID, "capacity must be at least 2 rows");
+        std::string why;
+        if (!check_model(q.p, q.p2, q.lambda, q.T0, q.Gamma, why)) return bfail(DYN_ERR_INVALID, why);
+    }
+    // every table on the host before any CUDA call
+    for (int g = 0; g < ngrids; ++g) {
+        std::vector<int> i32[3];
+        std::string why;
+        if (!check_tables(grids[g].len, grids[g].depth, &grids[g].tables, i32, why))
+            return bfail(DYN_ERR_INVALID, "grid " + std::to_string(g) + ": " + why);
     }
     if (cfg->precision != 0 && cfg->precision != DYN_MIXED && cfg->precision != DYN_MIXED_DF)
         return bfail(DYN_ERR_INVALID, "batch precision: DYN_MIXED or DYN_MIXED_DF");
@@ -925,9 +941,16 @@ dyn_status dyn_batch_upload(void* p, int qi, const dyn_state* stt, const dyn_con
     if (!stt->t1grid || !stt->delta_t_ratio || !stt->QK || !stt->QR || !stt->dQK || !stt->dQR || !stt->rvec || !stt->drvec)
         return bfail(DYN_ERR_INVALID, "missing state array");
     for (size_t k = 0; k < n; ++k) {
-        if (!(stt->t1grid[k] >= 0.0)) return bfail(DYN_ERR_INVALID, "t1grid must be non-negative");
+        if (!(stt->t1grid[k] >= 0.0) || !std::isfinite(stt->t1grid[k]))
+            return bfail(DYN_ERR_INVALID, "t1grid must be finite and non-negative");
         if (k && !(stt->t1grid[k] >= stt->t1grid[k - 1])) return bfail(DYN_ERR_INVALID, "t1grid must be non-decreasing");
+        if (!std::isfinite(stt->delta_t_ratio[k]) || !std::isfinite(stt->rvec[k]) || !std::isfinite(stt->drvec[k]))
+            return bfail(DYN_ERR_INVALID, "delta_t_ratio, rvec and drvec must be finite");
     }
+    for (size_t e = 0; e < n * L; ++e)
+        if (!std::isfinite(stt->QK[e]) || !std::isfinite(stt->QR[e]) || !std::isfinite(stt->dQK[e]) ||
+            !std::isfinite(stt->dQR[e]))
+            return bfail(DYN_ERR_INVALID, "QK, QR, dQK and dQR must be finite");
     if (ctl->method < 1 || ctl->method > 2 + QMAX / 2) return bfail(DYN_ERR_INVALID, "method out of range");
     if (!(ctl->delta_t > 0)) return bfail(DYN_ERR_INVALID, "delta_t must be positive");
     std::vector<double2> kr(n * L), dkr(n * L);
@@ -948,6 +971,7 @@ dyn_status dyn_batch_upload(void* p, int qi, const dyn_state* stt, const dyn_con
     BCK(launch_mirror_rows(q.c.KR, q.c.KRf, n * L, st));
     BCK(launch_mirror_rows(q.c.dKR, q.c.dKRf, n * L, st));
     if (q.c.KRl) BCK(launch_mirror_lo(q.c.KR, q.c.KRl, n * L, st));
+    BCK(clear_mirror_rows(q.c, n, (size_t)q.cap, st));  // whatever the previous history left
     BCK(launch_time_f32(q.c.t1grid, q.c.dtr, (int)n, q.c.inv_len_f, q.c.inv_dtr_f, st));
     Plan pl{};
     pl.status = DYN_QUENCH_RUNNING;

@@ -88,6 +88,7 @@ void set_last_error(const std::string& msg);
 
 // Validates a table set and returns the stencil starts as int32 (dyn_api.cu)
 bool check_tables(size_t L, size_t m, const dyn_tables* tb, std::vector<int> i32[3], std::string& why);
+bool check_model(int p, int p2, double lambda, double T0, double Gamma, std::string& why);
 
 // Keep list, derivative rows with their time factors, and the new t1grid /
 // delta_t_ratio of one sparsify pass from its node flags (dyn_api.cu); false

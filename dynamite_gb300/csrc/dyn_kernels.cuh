@@ -250,6 +250,11 @@ cudaError_t launch_pack_rows(const double* QK, const double* QR, double2* out, s
 cudaError_t launch_main_mixed(const DevCtx& c, int s, cudaStream_t st);
 cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cudaStream_t st);
 cudaError_t launch_mirror_lo(const double2* in, float2* out, size_t count, cudaStream_t st);
+// Rows past a history meet the zero taps of the mixed gathers' segment loads
+// (the element after a stencil window that ends a row is the next row's first),
+// so they must hold finite values: zero the FP32 mirror rows [r0, r1) that a
+// shortened or replaced history leaves behind (they may hold a failed step's NaN).
+cudaError_t clear_mirror_rows(const DevCtx& c, size_t r0, size_t r1, cudaStream_t st);
 cudaError_t launch_weights_tapmajor_lo(const double* in, float2* out, size_t targets, int m, cudaStream_t st);
 cudaError_t launch_weights_f32(const double* in, float* out, size_t count, cudaStream_t st);
 // [L*L][m] FP64 stencil rows to the tap-major FP32 pair planes of the mixed form

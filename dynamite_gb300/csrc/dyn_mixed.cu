@@ -138,6 +138,17 @@ cudaError_t launch_mirror_rows(const double2* in, float2* out, size_t count, cud
     return cudaGetLastError();
 }
 
+cudaError_t clear_mirror_rows(const DevCtx& c, size_t r0, size_t r1, cudaStream_t st) {
+    if (r1 <= r0) return cudaSuccess;
+    const size_t off = r0 * (size_t)c.L, bytes = (r1 - r0) * (size_t)c.L * sizeof(float2);
+    for (float2* p : {c.KRf, c.dKRf, c.KRl}) {
+        if (!p) continue;
+        const cudaError_t e = cudaMemsetAsync(p + off, 0, bytes, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr,
                             cudaStream_t st) {
     k_time_f32<<<(n + 255) / 256, 256, 0, st>>>(t1, dtr, n, inv_len, inv_dtr);

@@ -11,14 +11,19 @@
 // file-scope __device__ array of fixed size, allocated when the library is
 // loaded and held by every GPU that loads it until the process exits.
 //
-// Limits: len <= DYN_NOALLOC_MAX_LEN (1024), history rows <=
-// DYN_NOALLOC_MAX_ROWS (16384), stencil depth <= len.
+// Limits: 4 <= len <= DYN_NOALLOC_MAX_LEN (1024), 2 <= history rows <=
+// DYN_NOALLOC_MAX_ROWS (16384), 2 <= stencil depth <= len; the array is
+// DYN_NOALLOC_SCRATCH_BYTES (448 KiB).  The device tables are not read on
+// the host, so their stencil starts are the caller's to keep within
+// [0, len - depth] (dyn_check_tables checks host copies).
 //
 // Set-up: the first call on a device looks up the device address of the
 // array (cudaGetSymbolAddress, with that device current) and caches it for
-// that device; make that first call before any stream capture.  All calls
-// share the one array and it keeps the last call's contents; the parts that
-// must start at zero are cleared by every call.  Two calls whose kernels
+// that device for the rest of the process (a cudaDeviceReset of that device
+// would leave the cached address stale); make that first call before any
+// stream capture.  All calls share the one array and it keeps the last
+// call's contents; the parts that must start at zero are cleared by every
+// call.  Two calls whose kernels
 // overlap on the GPU (different streams, or different host threads on the
 // same device) race on the array: serialize them.
 #include <cstring>
@@ -56,8 +61,11 @@ constexpr size_t N_SLOTS = (sizeof(Slots) + 7) / 8 + 8;
 constexpr size_t OFF_STAGE = OFF_SLOTS + N_SLOTS;          // StageDev
 constexpr size_t N_STAGE = (sizeof(StageDev) + 7) / 8 + 8;
 constexpr size_t N_TOTAL = OFF_STAGE + N_STAGE;
+constexpr size_t N_ARRAY = DYN_NOALLOC_SCRATCH_BYTES / sizeof(double);
+static_assert(N_TOTAL <= N_ARRAY, "the scratch layout outgrows DYN_NOALLOC_SCRATCH_BYTES");
+static_assert(N_ARRAY * sizeof(double) == DYN_NOALLOC_SCRATCH_BYTES, "whole doubles");
 
-__device__ __align__(256) double g_noalloc_scratch[N_TOTAL];
+__device__ __align__(256) double g_noalloc_scratch[N_ARRAY];
 
 std::mutex g_mu;
 double* g_addr[64] = {nullptr};
@@ -94,9 +102,12 @@ extern "C" dyn_status dyn_rhs_noalloc(const dyn_noalloc_rhs* a, void* stream) {
     if (!a) return err(DYN_ERR_INVALID, "dyn_rhs_noalloc: null argument");
     if (a->len < 4 || a->len > (size_t)MAX_LEN)
         return err(DYN_ERR_INVALID, "dyn_rhs_noalloc: len must be in [4, DYN_NOALLOC_MAX_LEN=1024]");
-    if (a->rows < 1 || a->rows > (size_t)MAX_ROWS)
-        return err(DYN_ERR_INVALID, "dyn_rhs_noalloc: rows must be in [1, DYN_NOALLOC_MAX_ROWS=16384]");
+    // at least two rows: the B1/B2 clamps of a one-row history point at row 1
+    if (a->rows < 2 || a->rows > (size_t)MAX_ROWS)
+        return err(DYN_ERR_INVALID, "dyn_rhs_noalloc: rows must be in [2, DYN_NOALLOC_MAX_ROWS=16384]");
     if (a->depth < 2 || a->depth > a->len) return err(DYN_ERR_INVALID, "dyn_rhs_noalloc: bad stencil depth");
+    if (a->search != DYN_SEARCH_BINARY && a->search != DYN_SEARCH_LOWER_BOUND)
+        return err(DYN_ERR_INVALID, "dyn_rhs_noalloc: search must be DYN_SEARCH_BINARY or DYN_SEARCH_LOWER_BOUND");
     if (!a->theta || !a->phi2 || !a->integ || !a->indsA1y || !a->indsA2y || !a->indsB2y || !a->weightsA1y ||
         !a->weightsA2y || !a->weightsB2y || !a->KR || !a->dKR || !a->t1grid || !a->delta_t_ratio || !a->rvec ||
         !a->drvec || !a->out)

@@ -114,16 +114,47 @@ def _read(path: str, dtype=np.float64) -> np.ndarray:
         return np.array(fh.read().split(), dtype=dtype)
 
 
+def check(g: Grid) -> None:
+    """Raise ValueError unless the tables are complete and usable: every array of the size
+    its length L implies (weights L*L*depth with one depth for the three families), and
+    the host-side table check of the library (dyn_check_tables: theta on [0, 1] ending at
+    1, stencil starts within [0, L - depth], phi2 within [0, 1] ending at 1, finite
+    weights).  The reference reads the same files with no check (io_input.cpp:90-110)."""
+    L, L2 = g.L, g.L * g.L
+    sizes = dict(theta=L, integ=L, phi1=L2, phi2=L2, indsA1=L2, indsA2=L2, indsB2=L2)
+    for name, n in sizes.items():
+        a = getattr(g, name)
+        if a.size != n:
+            raise ValueError(f"grid L={L}: {name} holds {a.size} values, expected {n}")
+    if g.wA1.size % L2 or g.wA1.size // L2 < 2:
+        raise ValueError(f"grid L={L}: weightsA1y holds {g.wA1.size} values, not L*L*depth with depth >= 2")
+    m = g.wA1.size // L2
+    for name in ("wA2", "wB2"):
+        if getattr(g, name).size != L2 * m:
+            raise ValueError(f"grid L={L}: {name} holds {getattr(g, name).size} values, expected {L2 * m}")
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (g.theta, g.phi2, g.integ, g.wA1, g.wA2, g.wB2)]
+    i64 = [np.ascontiguousarray(a, dtype=np.int64) for a in (g.indsA1, g.indsA2, g.indsB2)]
+    tb = _lib.Tables(_lib.ptr(keep[0]), _lib.ptr(keep[1]), _lib.ptr(keep[2]), *[a.ctypes.data_as(_lib.i64p) for a in i64],
+                     *[_lib.ptr(a) for a in keep[3:]])
+    if _lib.lib().dyn_check_tables(L, m, tb) != _lib.DYN_OK:
+        raise ValueError(f"grid L={L}: " + _lib.lib().dyn_last_error().decode(errors="replace"))
+
+
 def load(directory: str) -> Grid:
-    """Read Grid_data/<L>/ as written by `RG-Evo grid`."""
+    """Read Grid_data/<L>/ as written by `RG-Evo grid`; a missing, truncated or
+    inconsistent table raises (OSError for a missing file, ValueError otherwise)."""
     th = _read(os.path.join(directory, "theta.dat"))
     L = th.size
+    if L < 4:
+        raise ValueError(f"{directory}: theta.dat holds {L} values (at least 4 needed)")
     p1_path = os.path.join(directory, "phi1.dat")
     p1 = _read(p1_path) if os.path.exists(p1_path) else np.zeros(L * L)
-    return Grid(L, th, p1, _read(os.path.join(directory, "phi2.dat")), _read(os.path.join(directory, "int.dat")),
-                _read(os.path.join(directory, "indsA1y.dat"), np.int64), _read(os.path.join(directory, "weightsA1y.dat")),
-                _read(os.path.join(directory, "indsA2y.dat"), np.int64), _read(os.path.join(directory, "weightsA2y.dat")),
-                _read(os.path.join(directory, "indsB2y.dat"), np.int64), _read(os.path.join(directory, "weightsB2y.dat")))
+    g = Grid(L, th, p1, _read(os.path.join(directory, "phi2.dat")), _read(os.path.join(directory, "int.dat")),
+             _read(os.path.join(directory, "indsA1y.dat"), np.int64), _read(os.path.join(directory, "weightsA1y.dat")),
+             _read(os.path.join(directory, "indsA2y.dat"), np.int64), _read(os.path.join(directory, "weightsA2y.dat")),
+             _read(os.path.join(directory, "indsB2y.dat"), np.int64), _read(os.path.join(directory, "weightsB2y.dat")))
+    check(g)
+    return g
 
 
 def save(g: Grid, directory: str) -> None:

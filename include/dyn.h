@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DYN_ABI_VERSION 3
+#define DYN_ABI_VERSION 4
 
 typedef enum {
     DYN_OK = 0,
@@ -32,7 +32,9 @@ typedef enum {
     DYN_ERR_NOMEM = -3,       /* device or host allocation failed */
     DYN_ERR_STATE = -4,       /* call not valid in the current state */
     DYN_ERR_UNSUPPORTED = -5, /* option not built into this library */
-    DYN_ERR_TIMEOUT = -6      /* a bounded device-side wait ran out */
+    DYN_ERR_NONFINITE = -6    /* a step's error estimate came out NaN or infinite: the state
+                                 holds non-finite values (overflow of the model terms); the
+                                 driver loop stops before its controller acts on it */
 } dyn_status;
 
 /* RK methods: values of rk->init (runge_kutta.cu:607-615). */
@@ -180,14 +182,27 @@ int dyn_abi_version(void);
 const char* dyn_last_error(void);
 
 /* Replaces import() + copyVectorsToGPU + copyParametersToDevice
- * (io_input.cpp:90-110, gpu_memory_utils.cu:11-146,195-199). */
+ * (io_input.cpp:90-110, gpu_memory_utils.cu:11-146,195-199).  Checks the
+ * model (finite lambda and Gamma, T0 > 0, exponents the kernels are built
+ * for) and the tables (dyn_check_tables) on the host before any CUDA call:
+ * a bad argument returns DYN_ERR_INVALID with the reason in dyn_last_error(). */
 dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tables, void** ctx);
+/* Host-side check of a grid's tables, no GPU needed (what dyn_ctx_create and
+ * dyn_batch_create run; io_input.cpp:90-110 reads the same files without a
+ * check): theta non-decreasing on [0, 1] with theta[len-1] == 1; every stencil
+ * start s of the three families within [0, len - depth], so that every tap
+ * s + d (d < depth) lies inside a history row; phi2 within [0, 1] ending at 1;
+ * finite weights and int.dat.  Returns DYN_ERR_INVALID with the first failure
+ * in dyn_last_error(). */
+dyn_status dyn_check_tables(size_t len, size_t depth, const dyn_tables* tables);
 dyn_status dyn_ctx_destroy(void* ctx);
 dyn_status dyn_sync(void* ctx);
 
 /* t=0 state: initialization.cpp:204-222 (+ the first interpolation, :267-274). */
 dyn_status dyn_state_init(void* ctx, double delta_t);
-/* Load / read back the history (loadSimulationState / copyVectorsToCPU). */
+/* Load / read back the history (loadSimulationState / copyVectorsToCPU).
+ * dyn_state_upload rejects (DYN_ERR_INVALID, nothing changed) a state whose
+ * t1grid is negative or decreasing or whose values are not all finite. */
 dyn_status dyn_state_upload(void* ctx, const dyn_state* st);
 dyn_status dyn_state_rows(void* ctx, size_t* n);
 /* t1grid of the newest row (the current time); 0 before any state */
@@ -242,7 +257,10 @@ dyn_status dyn_search_dev(void* ctx, const double* list, size_t nlist, const dou
 
 /* One RK step: updateGPU / update (runge_kutta.cu:607-615, runge_kutta.cpp:254-261). */
 dyn_status dyn_update(void* ctx, int method, double delta_t, dyn_step_result* res);
-/* The driver loop (simulation_runner.cpp:125-304) for p->nsteps iterations. */
+/* The driver loop (simulation_runner.cpp:125-304) for p->nsteps iterations.
+ * Returns DYN_ERR_NONFINITE (after storing that step's outputs) when a step's
+ * error estimate is NaN or infinite; the reference's loop would go on with
+ * it, its controller comparisons all false. */
 dyn_status dyn_run(void* ctx, const dyn_run_params* p, dyn_step_result* last);
 /* sparsifyNscale[GPU] (sparsify_utils.*): returns the new row count. */
 dyn_status dyn_sparsify(void* ctx, double threshold, int variant, size_t* n_out);
@@ -266,14 +284,23 @@ dyn_status dyn_probe_fp64(int device, double* gflops);
  * device pool it does not own, or one that has handed all free memory to its
  * history): every input and the output are the caller's device buffers, in
  * this library's layout; the kernels' scratch is a fixed file-scope device
- * array (about 0.5 MB per GPU, held from library load to process exit).
- * The first call on each device resolves that array's address (make it
- * before any stream capture); calls that overlap on the GPU race on it.
- * Limits: len <= DYN_NOALLOC_MAX_LEN, rows <= DYN_NOALLOC_MAX_ROWS;
- * larger sizes are rejected with DYN_ERR_INVALID.  Enqueued on `stream`
- * (cudaStream_t, NULL = default stream); the caller synchronizes. */
+ * array of DYN_NOALLOC_SCRATCH_BYTES per GPU, held from library load to
+ * process exit.  The first call on each device resolves that array's address
+ * (make it before any stream capture) and keeps it for the process: do not
+ * call across a cudaDeviceReset of that device.  Calls that overlap on the
+ * GPU race on the array: serialize them.
+ * Limits: 4 <= len <= DYN_NOALLOC_MAX_LEN, 2 <= rows <= DYN_NOALLOC_MAX_ROWS,
+ * 2 <= depth <= len, search DYN_SEARCH_BINARY or DYN_SEARCH_LOWER_BOUND;
+ * anything else is rejected with DYN_ERR_INVALID.
+ * The tables live in device memory and are NOT checked here: every stencil
+ * start must lie in [0, len - depth] (a larger one reads past a history row),
+ * theta and phi2 must be as dyn_check_tables requires.  Run dyn_check_tables
+ * on the host copies once before uploading them.
+ * Enqueued on `stream` (cudaStream_t, NULL = default stream); the caller
+ * synchronizes. */
 #define DYN_NOALLOC_MAX_LEN 1024
 #define DYN_NOALLOC_MAX_ROWS 16384
+#define DYN_NOALLOC_SCRATCH_BYTES 458752   /* 448 KiB */
 typedef struct {
     int p, p2;
     double lambda, T0, Gamma;
@@ -350,7 +377,9 @@ enum {
     DYN_QUENCH_DONE = 1,      /* reached t_stop */
     DYN_QUENCH_MAXSTEPS = 2,  /* took max_steps steps */
     DYN_QUENCH_FULL = 3,      /* history capacity reached */
-    DYN_QUENCH_SPARSIFY = 4   /* waiting for its periodic sparsify (transient) */
+    DYN_QUENCH_SPARSIFY = 4,  /* waiting for its periodic sparsify (transient) */
+    DYN_QUENCH_FAILED = 5     /* its error estimate came out NaN or infinite (as DYN_ERR_NONFINITE
+                                 of dyn_run); stopped until dyn_batch_upload gives it a new state */
 };
 
 typedef struct {

@@ -31,10 +31,44 @@ _i64p = C.POINTER(C.c_int64)
 _szp = C.POINTER(C.c_size_t)
 
 
+def reference_dir() -> str | None:
+    """The reference checkout the Makefile builds from (DYN_REFERENCE_DIR or the Makefile's
+    default), or None where its sources are absent (as on a GPU machine)."""
+    out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], check=True, capture_output=True, text=True)
+    d = out.stdout.strip()
+    return d or None
+
+
 def build(reference: bool = True) -> None:
-    """Compile the C restatement (and the reference where its sources exist)."""
+    """Compile the C restatement (and the reference where its sources exist), and write
+    the reference generator's L=512 poly-9 tables for the CPU baseline (reference_grid)."""
     target = "all" if reference else "port"
     subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+    if reference and os.path.exists(REF_LIB) and not os.path.exists(grid_cache_path(512)):
+        save_grid(Reference.grid(512), grid_cache_path(512))
+
+
+def grid_cache_path(L: int) -> str:
+    """Tables of `RG-Evo grid -L L -M 1e5 -s 5 -m poly -o 9` written by the reference's own
+    generator where it is built (oracle/_ref, beside the compiled reference)."""
+    return os.path.join(HERE, "_ref", f"grid_poly9_L{L}.npz")
+
+
+def save_grid(g: "Grid", path: str) -> None:
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp.npz"
+    np.savez(tmp, L=g.L, theta=g.theta, phi2=g.phi2, integ=g.integ,
+             indsA1=g.indsA1.astype(np.int32), indsA2=g.indsA2.astype(np.int32), indsB2=g.indsB2.astype(np.int32),
+             wA1=g.wA1, wA2=g.wA2, wB2=g.wB2)
+    os.replace(tmp, path)
+
+
+def load_grid(path: str) -> "Grid":
+    """A table set written by save_grid (phi1 is not read by the hot path: zeros)."""
+    with np.load(path) as f:
+        L = int(f["L"])
+        return Grid(L, f["theta"], np.zeros(L * L), f["phi2"], f["integ"], f["indsA1"].astype(np.int64), f["wA1"],
+                    f["indsA2"].astype(np.int64), f["wA2"], f["indsB2"].astype(np.int64), f["wB2"])
 
 
 def _d(a):

@@ -23,7 +23,7 @@ def load_golden(L: int) -> dict:
 @pytest.fixture(scope="session")
 def oracle_built():
     import oracle
-    oracle.build(reference=os.path.isdir("/root/reference/src"))
+    oracle.build()  # the reference part only where its sources exist
     return oracle
 
 

@@ -46,6 +46,19 @@ def _args(torch, grid, model, st, out, keep):
     return a
 
 
+def _check(torch, grid, model, st, hK, hR, keep, what):
+    out = torch.empty((grid.L, 2), dtype=torch.float64, device="cuda")
+    out.fill_(float("nan"))
+    args = _args(torch, grid, model, st, out, keep)
+    stream = torch.cuda.current_stream().cuda_stream
+    _lib.check(_lib.lib().dyn_rhs_noalloc(C.byref(args), stream), "dyn_rhs_noalloc")
+    torch.cuda.synchronize()
+    res = out.cpu().numpy()
+    assert np.isfinite(res).all(), what
+    assert rel_err(res[:, 0], hK) < RHS_TOL, what
+    assert rel_err(res[:, 1], hR) < RHS_TOL, what
+
+
 def test_rhs_noalloc_matches_rhs_on_two_calls():
     torch = pytest.importorskip("torch")
     g = load_golden(64)
@@ -67,6 +80,29 @@ def test_rhs_noalloc_matches_rhs_on_two_calls():
         assert np.isfinite(res).all()
         assert rel_err(res[:, 0], hK) < RHS_TOL, prefix
         assert rel_err(res[:, 1], hR) < RHS_TOL, prefix
+        if prefix == "mid":
+            # and the reference's own QKstep/QRstep of that state (the golden fixture)
+            assert rel_err(res[:, 0], g["mid_qk"]) < RHS_TOL
+            assert rel_err(res[:, 1], g["mid_qr"]) < RHS_TOL
+
+
+@pytest.mark.parametrize("L", [512, 1024])
+def test_rhs_noalloc_at_production_sizes(L):
+    """The scratch layout at the sizes it is sized for: L = 512 (4 targets per thread,
+    2 chunks per row) and L = 1024 (the largest length, 4 chunks per row), on a state
+    of 40 steps from t = 0 on the poly-9 grid, two calls in a row, against dyn_rhs."""
+    torch = pytest.importorskip("torch")
+    grid = D.grid.generate(L)
+    model = D.Model(p=3, p2=4, lam=0.5, Gamma=0.6)
+    sim = D.Simulation(grid, model)
+    sim.init()
+    sim.run(40)
+    st = sim.download()
+    hK, hR = sim.rhs()
+    keep = []
+    for call in range(2):
+        _check(torch, grid, model, st, hK, hR, keep, f"L={L} call {call}")
+    sim.close()
 
 
 def test_rhs_noalloc_rejects_sizes_beyond_its_scratch():
@@ -76,3 +112,10 @@ def test_rhs_noalloc_rejects_sizes_beyond_its_scratch():
     b = _lib.NoAllocRHS(3, 4, 0.5, 1e50, 0.6, 64, 10, 20000, 0)
     assert _lib.lib().dyn_rhs_noalloc(C.byref(b), None) == -1
     assert b"DYN_NOALLOC_MAX_ROWS" in _lib.lib().dyn_last_error()
+    # a one-row history (its B1/B2 clamps would point at row 1) and an unknown search
+    c = _lib.NoAllocRHS(3, 4, 0.5, 1e50, 0.6, 64, 10, 1, 0)
+    assert _lib.lib().dyn_rhs_noalloc(C.byref(c), None) == -1
+    assert b"rows" in _lib.lib().dyn_last_error()
+    d = _lib.NoAllocRHS(3, 4, 0.5, 1e50, 0.6, 64, 10, 10, 2)
+    assert _lib.lib().dyn_rhs_noalloc(C.byref(d), None) == -1
+    assert b"search" in _lib.lib().dyn_last_error()
