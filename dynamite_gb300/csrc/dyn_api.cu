@@ -542,6 +542,11 @@ bool check_tables(size_t L, size_t m, const dyn_tables* tb, std::vector<int> i32
     }
     for (size_t e = 0; e < L2; ++e)
         if (!(tb->phi2[e] >= 0.0 && tb->phi2[e] <= 1.0)) { why = "phi2 outside [0, 1]"; return false; }
+    // phi2[i][j] = theta_i + (1 - theta_i) theta_j grows along a row; the mixed gathers
+    // bracket their interval searches on that
+    for (size_t i = 0; i < L; ++i)
+        for (size_t j = 1; j < L; ++j)
+            if (tb->phi2[i * L + j] < tb->phi2[i * L + j - 1]) { why = "phi2 rows must be non-decreasing"; return false; }
     if (tb->phi2[L2 - 1] != 1.0) { why = "phi2 must end at 1"; return false; }
     for (size_t i = 0; i < L; ++i)
         if (!std::isfinite(tb->integ[i])) { why = "int.dat holds a non-finite weight"; return false; }

@@ -13,6 +13,29 @@ struct FModel {
     float cA, cB, cC, cD;
 };
 
+// Packed FP32x2 arithmetic (fma.rn.f32x2 / mul.rn.f32x2 of the sm_100 family): one
+// instruction for the (QK, QR) pair, each half rounded exactly as fmaf / __fmul_rn.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+// w * x + c for both halves of x and c
+__device__ __forceinline__ float2 ffma2s(float w, float2 x, float2 c) { return ffma2(make_float2(w, w), x, c); }
+__device__ __forceinline__ float2 fmul2s(float w, float2 x) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %2};\n\tmov.b64 rb, {%3, %4};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(w), "f"(x.x), "f"(x.y));
+    return d;
+}
+
 template <int E>
 __device__ __forceinline__ float fpow_c(float q) {
     if constexpr (E <= 0) return 1.0f;
@@ -55,12 +78,10 @@ __device__ __forceinline__ float2 dotfT(const float2* __restrict__ w, size_t L2,
     for (int d = 0; d < m; d += 2) {
         const float2 ww = __ldg(w + (size_t)(d >> 1) * L2 + ij);
         const float2 xa = ldg ? __ldg(x + d) : x[d];
-        acc.x = fmaf(ww.x, xa.x, acc.x);
-        acc.y = fmaf(ww.x, xa.y, acc.y);
+        acc = ffma2s(ww.x, xa, acc);
         if (d + 1 < m) {
             const float2 xb = ldg ? __ldg(x + d + 1) : x[d + 1];
-            acc.x = fmaf(ww.y, xb.x, acc.x);
-            acc.y = fmaf(ww.y, xb.y, acc.y);
+            acc = ffma2s(ww.y, xb, acc);
         }
     }
     return acc;
@@ -83,11 +104,7 @@ __device__ __forceinline__ float2 seg10(const float w[10], const float2* __restr
     }
     float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int d = 0; d < 10; ++d) {
-        const float2 x = sh ? e[d + 1] : e[d];
-        acc.x = fmaf(w[d], x.x, acc.x);
-        acc.y = fmaf(w[d], x.y, acc.y);
-    }
+    for (int d = 0; d < 10; ++d) acc = ffma2s(w[d], sh ? e[d + 1] : e[d], acc);
     return acc;
 }
 __device__ __forceinline__ float2 seg10s(const float w[10], const float2* arr, int b) {
@@ -103,11 +120,7 @@ __device__ __forceinline__ float2 seg10s(const float w[10], const float2* arr, i
     }
     float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int d = 0; d < 10; ++d) {
-        const float2 x = sh ? e[d + 1] : e[d];
-        acc.x = fmaf(w[d], x.x, acc.x);
-        acc.y = fmaf(w[d], x.y, acc.y);
-    }
+    for (int d = 0; d < 10; ++d) acc = ffma2s(w[d], sh ? e[d + 1] : e[d], acc);
     return acc;
 }
 
@@ -132,15 +145,10 @@ __device__ __forceinline__ float2 seg11(const float w11[11], const float2* __res
 #pragma unroll
     for (int q = 0; q < 5; ++q) {
         const float4 v = __ldg(p + q);
-        acc.x = fmaf(w11[2 * q], v.x, acc.x);
-        acc.y = fmaf(w11[2 * q], v.y, acc.y);
-        acc.x = fmaf(w11[2 * q + 1], v.z, acc.x);
-        acc.y = fmaf(w11[2 * q + 1], v.w, acc.y);
+        acc = ffma2s(w11[2 * q], make_float2(v.x, v.y), acc);
+        acc = ffma2s(w11[2 * q + 1], make_float2(v.z, v.w), acc);
     }
-    const float2 e = __ldg(arr + a + 10);
-    acc.x = fmaf(w11[10], e.x, acc.x);
-    acc.y = fmaf(w11[10], e.y, acc.y);
-    return acc;
+    return ffma2s(w11[10], __ldg(arr + a + 10), acc);
 }
 
 // The same segment from shared memory (the staged last row)
@@ -150,15 +158,10 @@ __device__ __forceinline__ float2 seg11s(const float w11[11], const float2* arr,
 #pragma unroll
     for (int q = 0; q < 5; ++q) {
         const float4 v = p[q];
-        acc.x = fmaf(w11[2 * q], v.x, acc.x);
-        acc.y = fmaf(w11[2 * q], v.y, acc.y);
-        acc.x = fmaf(w11[2 * q + 1], v.z, acc.x);
-        acc.y = fmaf(w11[2 * q + 1], v.w, acc.y);
+        acc = ffma2s(w11[2 * q], make_float2(v.x, v.y), acc);
+        acc = ffma2s(w11[2 * q + 1], make_float2(v.z, v.w), acc);
     }
-    const float2 e = arr[a + 10];
-    acc.x = fmaf(w11[10], e.x, acc.x);
-    acc.y = fmaf(w11[10], e.y, acc.y);
-    return acc;
+    return ffma2s(w11[10], arr[a + 10], acc);
 }
 
 // the ten taps of target ij from the tap-major planes
@@ -219,43 +222,36 @@ __device__ __forceinline__ void warp_reduce8_pair(const float hv[8], const float
     Lo = yl;
 }
 
-// Binary search of bsearchPosSorted (the same probes as pos_binary), returning
-// floor(position) as an integer and the offset from it in FP32.
-__device__ __forceinline__ void pos_split(const ListView& L, const float* __restrict__ inv_len, double El,
-                                          int& X, float& x) {
-    int n0 = 1, n1 = L.n, m = 1;
-    double Lm = 0.0;
+// The interval of El in the time list: the largest k in [lo, hi] with list[k] <= El
+// (exact: integer compares on the bit patterns of the non-negative FP64 times).  The
+// caller brackets the answer: list[lo] <= El (or lo = 0) and k(El) <= hi.
+__device__ __forceinline__ int floor_index(const ListView& L, double El, int lo, int hi) {
     const long long kE = okey(El);
-    if (okey(L.at(0)) < kE) {
-        while (n0 <= n1) {
-            m = (n0 + n1) >> 1;
-            Lm = L.at(m - 1);
-            const long long k = okey(Lm);
-            if (k == kE) { n0 = m; break; }
-            if (k < kE) n0 = m + 1; else n1 = m - 1;
-        }
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (okey(L.at(mid)) <= kE) lo = mid;
+        else hi = mid - 1;
     }
-    if (okey(Lm) <= kE) {
-        if (m == L.n) { X = m; x = 0.f; return; }
-        // interval [list[m-1], list[m]]: one FP64 difference, FP32 scale
-        const float f = (float)(El - Lm) * __ldg(inv_len + (m - 1));
-        if (f >= 1.0f) { X = m + 1; x = f - 1.0f; } else { X = m; x = f; }
-        return;
-    }
-    if (m > 1) {
-        // interval [list[m-2], list[m-1]], position m - f
-        const float f = (float)(Lm - El) * __ldg(inv_len + (m - 2));
-        if (f > 0.0f) { X = m - 1; x = 1.0f - f; } else { X = m; x = -f; }
-        return;
-    }
-    X = m;
-    x = 0.f;
+    return lo;
+}
+
+// The 1-based position of El in the list split into floor X and FP32 offset x from
+// its interval k: X = k + 1, x = (El - list[k]) / (list[k+1] - list[k]) with one
+// FP64 difference scaled by the stored FP32 inverse length (El at or past the last
+// entry: X = n, x = 0).
+__device__ __forceinline__ void split_at(const ListView& L, const float* __restrict__ inv_len, double El, int k,
+                                         int& X, float& x) {
+    if (k >= L.n - 1) { X = L.n; x = 0.f; return; }
+    const float f = (float)(El - L.at(k)) * __ldg(inv_len + k);
+    if (f >= 1.0f) { X = k + 2; x = f - 1.0f; } else { X = k + 1; x = f; }
 }
 
 
 // Block-shared scratch of one target row
 constexpr int RED_CAP = 512;  // per-warp partial sums held between folds (doubles)
+constexpr int MAX_SEG = 4096 / 32;  // 32-target segments of the longest row
 struct RowShared {
+    int seg[MAX_SEG + 1];  // B2 interval brackets: seg[w] = k(phi2[i][32 w] t), seg[nseg] = k(phi2[i][L-1] t)
     float c[4];            // B1 Hermite constants of the row (FP32)
     int bi[2];             // B1 floor index, cubic flag
     float2 red[RED_CAP];   // [chunk slot][warp][8] partial sums as (hi, lo)
@@ -315,6 +311,17 @@ __device__ __forceinline__ void row_setup(const DevCtx& c, const StageDev& sp, c
             if (first) c.rowval[i] = make_double2(c.KR[0].x, c.rvec[0]);
         }
         if (i == 0 && first) c.slots->q0 = c.KR[(size_t)(nrows - 1) * L].x;
+    }
+    // B2 brackets: phi2 is non-decreasing along a row (checked when the tables are
+    // loaded), so every target of 32-target segment w has its interval in
+    // [seg[w], seg[w + 1]]; one full search per segment, short ones per target
+    if (live) {
+        const int nseg = (L + 31) >> 5;
+        const ListView lv{c.t1grid, nrows, t};
+        for (int w = threadIdx.x; w <= nseg; w += tpb) {
+            const int j = w < nseg ? (w << 5) : L - 1;
+            sh.seg[w] = floor_index(lv, __dmul_rn(c.phi2[(size_t)i * L + j], t), 0, nrows - 1);
+        }
     }
     if (threadIdx.x == 32 && first && sp.kind != KIND_RHS && sp.pos_reuse < 0) {
         // next stage's B1 position of this row (the row this stage writes
@@ -381,18 +388,16 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
                     const float2 x0 = __ldg(c.KRf + (size_t)(F - 1) * L + j);
                     const float2 x1 = __ldg(c.KRf + (size_t)F * L + j);
                     const float2 d1 = __ldg(c.dKRf + (size_t)F * L + j);
-                    b1.x = bc0 * x0.x + bc1 * x1.x - bc2 * d1.x;
-                    b1.y = bc0 * x0.y + bc1 * x1.y - bc2 * d1.y;
-                    if (cubic1) {
-                        const float2 d2 = __ldg(c.dKRf + (size_t)(F + 1) * L + j);
-                        b1.x -= bc3 * d2.x;
-                        b1.y -= bc3 * d2.y;
-                    }
+                    // c0 x0 + c1 x1 - c2 d1 (- c3 d2), packed over (QK, QR)
+                    float2 r = fmul2s(-bc2, d1);
+                    if (cubic1) r = ffma2s(-bc3, __ldg(c.dKRf + (size_t)(F + 1) * L + j), r);
+                    b1 = ffma2s(bc0, x0, ffma2s(bc1, x1, r));
                 }
                 {
                     int X;
                     float x;
-                    pos_split(lv, c.inv_len_f, __dmul_rn(__ldg(c.phi2 + ij), t), X, x);
+                    const double El = __dmul_rn(__ldg(c.phi2 + ij), t);
+                    split_at(lv, c.inv_len_f, El, floor_index(lv, El, sh.seg[j >> 5], sh.seg[(j >> 5) + 1]), X, x);
                     if (X > maxX) { x += __int2float_rn(X - maxX); X = maxX; }
                     if (X < 1) { x -= __int2float_rn(1 - X); X = 1; }
                     const float x2 = x * x, x3 = x2 * x;
@@ -426,12 +431,10 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
                         const float e0 = 1.f - 3.f * x2 + 2.f * x3, e1 = x - 2.f * x2 + x3;
                         const float e2 = 3.f * x2 - 2.f * x3;
                         const float e3 = (x3 - x2) * __ldg(c.inv_dtr_f + X + 1);
-                        b2.x = e0 * S0.x + e1 * D1.x + e2 * S1.x + e3 * D2.x;
-                        b2.y = e0 * S0.y + e1 * D1.y + e2 * S1.y + e3 * D2.y;
+                        b2 = ffma2s(e0, S0, ffma2s(e1, D1, ffma2s(e2, S1, fmul2s(e3, D2))));
                     } else {
                         const float e0 = 1.f - x2, e2 = x - x2;
-                        b2.x = e0 * S0.x + x2 * S1.x + e2 * D1.x;
-                        b2.y = e0 * S0.y + x2 * S1.y + e2 * D1.y;
+                        b2 = ffma2s(e0, S0, ffma2s(x2, S1, fmul2s(e2, D1)));
                     }
                 }
             } else {
@@ -639,7 +642,8 @@ __device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const
                 {
                     int X;
                     float x;
-                    pos_split(lv, c.inv_len_f, __dmul_rn(__ldg(c.phi2 + ij), t), X, x);
+                    const double El = __dmul_rn(__ldg(c.phi2 + ij), t);
+                    split_at(lv, c.inv_len_f, El, floor_index(lv, El, sh.seg[j >> 5], sh.seg[(j >> 5) + 1]), X, x);
                     if (X > maxX) { x += __int2float_rn(X - maxX); X = maxX; }
                     if (X < 1) { x -= __int2float_rn(1 - X); X = 1; }
                     const float x2 = x * x, x3 = x2 * x;
