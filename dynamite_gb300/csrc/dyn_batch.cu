@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(TPB, DF ? DYN_BATCH_DF_TPSM / TPB : (K == 1 ? 
                 const int ng = min(GMAX, nch - ch0);
                 for (int g = 0; g < ng; ++g) {
                     if constexpr (DF) mdf::chunk<M, K, P, P2>(q.c, sp, ch0 + g, g, s_lastf, s_lo, s_clo, sh, i);
-                    else mixed::chunk_sums<M, K, P, P2, DYN_BATCH_SHIFT != 0>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
+                    else mixed::chunk_sums<M, K, P, P2, DYN_BATCH_SHIFT>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
                 }
                 __syncthreads();
                 mixed::fold_chunks(q.c, i, nch, ch0, ng, sh);

@@ -336,9 +336,10 @@ __device__ __forceinline__ void row_setup(const DevCtx& c, const StageDev& sp, c
 // TwoSum accumulation; each warp's eight sums land in sh.red[slot][warp].
 // Call after row_setup and a __syncthreads(); no barrier inside, so a block
 // can run several chunks (slots) before one fold.
-// SHIFT picks the segment form for depth 10 (shifted weights, seg11, or
-// per-tap selects, seg10): same results, different register footprints.
-template <int M, int K, int P, int P2, bool SHIFT = true>
+// SHIFT picks the segment form for depth 10, bit 0 for the A1/A2 gathers and bit 1
+// for B2 (set: shifted weights, seg11; clear: per-tap selects, seg10): same
+// results, different instruction counts and register footprints.
+template <int M, int K, int P, int P2, int SHIFT = 3>
 __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, const int ch, const int slot,
                                            const float2* s_lastf, RowShared& sh, const int i) {
     const int L = c.L, tpb = blockDim.x;
@@ -365,7 +366,7 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
             const size_t ij = (size_t)i * L + j;
             float2 a1, a2, b1, b2;
             if (live) {
-                if constexpr (M == 10 && SHIFT) {
+                if constexpr (M == 10 && (SHIFT & 1)) {
                     float wv[10], w11[11];
                     const int sa1 = __ldg(c.iA1 + ij), sa2 = __ldg(c.iA2 + ij);
                     load_w10(c.wA1f, L2, ij, wv);
@@ -402,40 +403,36 @@ __device__ __forceinline__ void chunk_sums(const DevCtx& c, const StageDev& sp, 
                     if (X < 1) { x -= __int2float_rn(1 - X); X = 1; }
                     const float x2 = x * x, x3 = x2 * x;
                     const size_t base = (size_t)(X - 1) * (size_t)L + (size_t)__ldg(c.iB2 + ij);
-                    float2 S0, S1, D1, D2 = make_float2(0.f, 0.f);
                     const bool cubic2 = X < nrows - 1;
-                    if constexpr (M == 10 && SHIFT) {
+                    // the four 10-tap segments (rows X-1, X of (QK, QR), rows X, X+1 of (dQK, dQR)),
+                    // each folded into the Hermite sum as it completes
+                    [[maybe_unused]] float w11[11];
+                    [[maybe_unused]] float wv[10];
+                    if constexpr (M == 10) {
                         // even L (the M == 10 kernels require it): every segment start has base's parity
-                        float wv[10], w11[11];
                         load_w10(c.wB2f, L2, ij, wv);
-                        shift_w(wv, base & 1, w11);
-                        const size_t a = base & ~(size_t)1;
-                        S0 = seg11(w11, c.KRf, a);
-                        S1 = seg11(w11, c.KRf, a + L);
-                        D1 = seg11(w11, c.dKRf, a + L);
-                        if (cubic2) D2 = seg11(w11, c.dKRf, a + 2 * L);
-                    } else if constexpr (M == 10) {
-                        float wv[10];
-                        load_w10(c.wB2f, L2, ij, wv);
-                        S0 = seg10(wv, c.KRf, base);
-                        S1 = seg10(wv, c.KRf, base + L);
-                        D1 = seg10(wv, c.dKRf, base + L);
-                        if (cubic2) D2 = seg10(wv, c.dKRf, base + 2 * L);
-                    } else {
-                        S0 = dotfT(c.wB2f, L2, ij, c.KRf + base, m, true);
-                        S1 = dotfT(c.wB2f, L2, ij, c.KRf + base + L, m, true);
-                        D1 = dotfT(c.wB2f, L2, ij, c.dKRf + base + L, m, true);
-                        if (cubic2) D2 = dotfT(c.wB2f, L2, ij, c.dKRf + base + 2 * L, m, true);
+                        if constexpr ((SHIFT & 2) != 0) shift_w(wv, base & 1, w11);
                     }
+                    auto seg = [&](const float2* __restrict__ arr, size_t off) -> float2 {
+                        if constexpr (M == 10 && (SHIFT & 2)) return seg11(w11, arr, (base & ~(size_t)1) + off);
+                        else if constexpr (M == 10) return seg10(wv, arr, base + off);
+                        else return dotfT(c.wB2f, L2, ij, arr + base + off, m, true);
+                    };
+                    float2 r;
+                    float e0;
                     if (cubic2) {
-                        const float e0 = 1.f - 3.f * x2 + 2.f * x3, e1 = x - 2.f * x2 + x3;
-                        const float e2 = 3.f * x2 - 2.f * x3;
+                        e0 = 1.f - 3.f * x2 + 2.f * x3;
+                        const float e1 = x - 2.f * x2 + x3, e2 = 3.f * x2 - 2.f * x3;
                         const float e3 = (x3 - x2) * __ldg(c.inv_dtr_f + X + 1);
-                        b2 = ffma2s(e0, S0, ffma2s(e1, D1, ffma2s(e2, S1, fmul2s(e3, D2))));
+                        r = fmul2s(e3, seg(c.dKRf, 2 * (size_t)L));
+                        r = ffma2s(e2, seg(c.KRf, L), r);
+                        r = ffma2s(e1, seg(c.dKRf, L), r);
                     } else {
-                        const float e0 = 1.f - x2, e2 = x - x2;
-                        b2 = ffma2s(e0, S0, ffma2s(x2, S1, fmul2s(e2, D1)));
+                        e0 = 1.f - x2;
+                        r = fmul2s(x - x2, seg(c.dKRf, L));
+                        r = ffma2s(x2, seg(c.KRf, L), r);
                     }
+                    b2 = ffma2s(e0, seg(c.KRf, 0), r);
                 }
             } else {
                 a1 = a2 = b1 = b2 = fill;
