@@ -131,6 +131,13 @@ DYN_QUENCH_RUNNING, DYN_QUENCH_DONE, DYN_QUENCH_MAXSTEPS, DYN_QUENCH_FULL = 0, 1
 _lib = None
 
 
+class StateDev(C.Structure):
+    """dyn_state_dev: the history in the reference's device layout (device pointers)."""
+
+    _fields_ = [("n", C.c_size_t)] + [(f, C.c_void_p) for f in ("t1grid", "delta_t_ratio", "QK", "QR", "dQK", "dQR",
+                                                                 "rvec", "drvec")]
+
+
 class DynError(RuntimeError):
     """A dyn_status other than DYN_OK; `status` holds the code."""
 
@@ -185,6 +192,11 @@ def lib():
             "dyn_profile_stage": ([vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
             "dyn_probe_fp64": ([C.c_int, dp], C.c_int),
             "dyn_rhs_noalloc": ([C.POINTER(NoAllocRHS), vp], C.c_int),
+            "dyn_state_upload_dev": ([vp, C.POINTER(StateDev)], C.c_int),
+            "dyn_state_rows_load_dev": ([vp, C.c_size_t, C.c_size_t, C.POINTER(StateDev)], C.c_int),
+            "dyn_state_rows_store_dev": ([vp, C.c_size_t, C.c_size_t, C.POINTER(StateDev)], C.c_int),
+            "dyn_get_interp_dev": ([vp, C.c_int, vp], C.c_int),
+            "dyn_interp_b1_dev": ([vp, vp, vp], C.c_int),
             "dyn_batch_create": ([C.POINTER(BatchConfig), C.POINTER(BatchGrid), C.c_int, C.POINTER(BatchQuench),
                                   C.c_int, C.POINTER(vp)], C.c_int),
             "dyn_batch_destroy": ([vp], C.c_int),

@@ -1031,6 +1031,111 @@ dyn_status dyn_get_interp(void* p, int which, double* out) {
     return DYN_OK;
 }
 
+dyn_status dyn_get_interp_dev(void* p, int which, double* out) {
+    if (!p || !out) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    const double* src;
+    size_t count;
+    if (which >= 0 && which < 16) {
+        if (!c->interp_alloc) return fail(DYN_ERR_STATE, "call dyn_interpolate first");
+        src = c->d.ip + (size_t)which * c->L2;
+        count = c->L2;
+    } else if (which == DYN_RINT) { src = c->d.rint; count = c->L; }
+    else if (which == DYN_POSB1X) { src = c->d.posB1x; count = c->L; }
+    else if (which == DYN_POSB2X) { src = c->d.posB2x; count = c->L2; }
+    else return fail(DYN_ERR_INVALID, "unknown array");
+    CK(cudaMemcpyAsync(out, src, count * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_interp_b1_dev(void* p, double* qk, double* qr) {
+    if (!p || !qk || !qr) return fail(DYN_ERR_INVALID, "null argument");
+    Ctx* c = C(p);
+    if (c->n == 0) return fail(DYN_ERR_STATE, "no state");
+    CK(launch_b1_exact(c->d, (int)c->n, qk, qr, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+static bool state_dev_complete(const dyn_state_dev* s) {
+    return s && s->t1grid && s->delta_t_ratio && s->QK && s->QR && s->dQK && s->dQR && s->rvec && s->drvec;
+}
+
+dyn_status dyn_state_upload_dev(void* p, const dyn_state_dev* stt) {
+    if (!p || !state_dev_complete(stt)) return fail(DYN_ERR_INVALID, "null argument or missing state array");
+    Ctx* c = C(p);
+    const size_t n = stt->n, L = c->L;
+    if (n < 1) return fail(DYN_ERR_INVALID, "state needs at least one row");
+    std::vector<double> t1(n), dtr(n);
+    CK(cudaMemcpyAsync(t1.data(), stt->t1grid, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(dtr.data(), stt->delta_t_ratio, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t k = 0; k < n; ++k) {
+        if (!(t1[k] >= 0.0) || !std::isfinite(t1[k])) return fail(DYN_ERR_INVALID, "t1grid must be finite and non-negative");
+        if (k && !(t1[k] >= t1[k - 1])) return fail(DYN_ERR_INVALID, "t1grid must be non-decreasing");
+        if (!std::isfinite(dtr[k])) return fail(DYN_ERR_INVALID, "delta_t_ratio must be finite");
+    }
+    c->drop_graphs();
+    c->gen++;
+    const size_t n_old = c->n;
+    c->n = 0;
+    dyn_status s = c->ensure_rows(n + 1);
+    if (s) return s;
+    CK(launch_pack_rows(stt->QK, stt->QR, c->d.KR, n * L, c->st));
+    CK(launch_pack_rows(stt->dQK, stt->dQR, c->d.dKR, n * L, c->st));
+    CK(cudaMemcpyAsync(c->d.rvec, stt->rvec, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.drvec, stt->drvec, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+    c->n = n;
+    c->t1 = std::move(t1);
+    c->dtr = std::move(dtr);
+    if ((s = c->mirror_all())) return s;
+    if ((s = c->clear_tail(n_old))) return s;
+    if ((s = c->upload_times())) return s;
+    if ((s = c->pos_init())) return s;
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_state_rows_load_dev(void* p, size_t row0, size_t nrows, const dyn_state_dev* src) {
+    if (!p || !state_dev_complete(src)) return fail(DYN_ERR_INVALID, "null argument or missing state array");
+    Ctx* c = C(p);
+    const size_t L = c->L;
+    if (nrows == 0 || row0 + nrows > c->n) return fail(DYN_ERR_INVALID, "rows outside the history");
+    const size_t o = row0 * L, cnt = nrows * L;
+    CK(launch_pack_rows(src->QK + o, src->QR + o, c->d.KR + o, cnt, c->st));
+    CK(launch_pack_rows(src->dQK + o, src->dQR + o, c->d.dKR + o, cnt, c->st));
+    CK(cudaMemcpyAsync(c->d.rvec + row0, src->rvec + row0, nrows * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.drvec + row0, src->drvec + row0, nrows * sizeof(double), cudaMemcpyDeviceToDevice,
+                       c->st));
+    if (c->d.mixed) {
+        CK(launch_mirror_rows(c->d.KR + o, c->d.KRf + o, cnt, c->st));
+        CK(launch_mirror_rows(c->d.dKR + o, c->d.dKRf + o, cnt, c->st));
+        if (c->d.KRl) CK(launch_mirror_lo(c->d.KR + o, c->d.KRl + o, cnt, c->st));
+    }
+    c->gen++;
+    CK(cudaStreamSynchronize(c->st));
+    return DYN_OK;
+}
+
+dyn_status dyn_state_rows_store_dev(void* p, size_t row0, size_t nrows, const dyn_state_dev* dst) {
+    if (!p || !state_dev_complete(dst)) return fail(DYN_ERR_INVALID, "null argument or missing state array");
+    Ctx* c = C(p);
+    const size_t L = c->L;
+    if (nrows == 0 || row0 + nrows > c->n) return fail(DYN_ERR_INVALID, "rows outside the history");
+    const size_t o = row0 * L, cnt = nrows * L;
+    CK(launch_unpack_rows(c->d.KR + o, dst->QK + o, dst->QR + o, cnt, c->st));
+    CK(launch_unpack_rows(c->d.dKR + o, dst->dQK + o, dst->dQR + o, cnt, c->st));
+    CK(cudaMemcpyAsync(dst->t1grid + row0, c->t1.data() + row0, nrows * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(dst->delta_t_ratio + row0, c->dtr.data() + row0, nrows * sizeof(double),
+                       cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(dst->rvec + row0, c->d.rvec + row0, nrows * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(dst->drvec + row0, c->d.drvec + row0, nrows * sizeof(double), cudaMemcpyDeviceToDevice,
+                       c->st));
+    CK(cudaStreamSynchronize(c->st));  // the host time mirrors are the copies' sources
+    return DYN_OK;
+}
+
 dyn_status dyn_qkr_step(void* p, double* hK, double* hR) {
     if (!p || !hK || !hR) return fail(DYN_ERR_INVALID, "null argument");
     Ctx* c = C(p);

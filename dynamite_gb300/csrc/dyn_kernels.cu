@@ -331,6 +331,56 @@ __global__ void k_pos_b1_exact(const DevCtx c, const int nrows, const double* po
     }
 }
 
+// B1 (index_vec.cpp:63-136): C and R at time theta_i t, column j, by the cubic
+// (quadratic at the last interval) Hermite of the history rows around posB1x[i],
+// in the reference's operation order; log space for R with the -R option
+__device__ __forceinline__ void b1_exact(const DevCtx& c, const int nrows, const int maxceil, const int i, const int j,
+                                         double& vK, double& vR) {
+    const int L = c.L;
+    const double pos = c.posB1x[i];
+    long long F = (long long)floor(pos);
+    if (F < 1) F = 1; else if (F > maxceil) F = maxceil;
+    const double wt = sub((double)F, pos);
+    const double in3 = mul(wt, wt), in4 = mul(in3, wt);
+    const double2 x0 = c.KR[(size_t)(F - 1) * L + j], x1 = c.KR[(size_t)F * L + j];
+    const double2 d1 = c.dKR[(size_t)F * L + j];
+    if (F < nrows - 1) {
+        const double2 d2 = c.dKR[(size_t)(F + 1) * L + j];
+        const double dr = c.dtr[F + 1];
+        const double e0 = sub(sub(1.0, mul(3.0, in3)), mul(2.0, in4));
+        const double e1 = add(mul(3.0, in3), mul(2.0, in4));
+        const double e2 = add(add(wt, mul(2.0, in3)), in4);
+        const double e3 = add(in3, in4);
+        vK = sub(sub(add(mul(e0, x0.x), mul(e1, x1.x)), mul(e2, d1.x)), dvd(mul(e3, d2.x), dr));
+        vR = sub(sub(add(mul(e0, x0.y), mul(e1, x1.y)), mul(e2, d1.y)), dvd(mul(e3, d2.y), dr));
+        if (c.logr && x0.y > 0.0 && x1.y > 0.0)  // index_vec.cpp:89-100
+            vR = exp(sub(sub(add(mul(e0, log(x0.y)), mul(e1, log(x1.y))), mul(e2, dvd(d1.y, x0.y))),
+                         mul(dvd(e3, dr), dvd(d2.y, x1.y))));
+    } else {
+        const double e0 = sub(1.0, in3), e2 = add(wt, in3);
+        vK = add(sub(mul(e0, x0.x), mul(e2, d1.x)), mul(in3, x1.x));
+        vR = add(sub(mul(e0, x0.y), mul(e2, d1.y)), mul(in3, x1.y));
+        if (c.logr && x0.y > 0.0 && x1.y > 0.0)  // index_vec.cpp:122-127
+            vR = exp(sub(add(mul(e0, log(x0.y)), mul(in3, log(x1.y))), mul(e2, dvd(d1.y, x0.y))));
+    }
+}
+
+// The B1 pair alone (what a save of the reference reads back as QK_B1/QR_B1), into
+// caller arrays [L*L]; the t = 0 state gives the single row's values
+__global__ void k_b1_exact(const DevCtx c, const int nrows, double* qk, double* qr) {
+    const int L = c.L;
+    const size_t L2 = (size_t)L * L;
+    const bool live = c.t1grid[nrows - 1] > 0.0;
+    const int maxceil = c.slots->maxceil;
+    for (size_t ij = (size_t)blockIdx.x * blockDim.x + threadIdx.x; ij < L2; ij += (size_t)gridDim.x * blockDim.x) {
+        double vK, vR;
+        if (live) b1_exact(c, nrows, maxceil, (int)(ij / L), (int)(ij % L), vK, vR);
+        else { vK = c.KR[0].x; vR = c.KR[0].y; }
+        qk[ij] = vK;
+        qr[ij] = vR;
+    }
+}
+
 __global__ void k_interp_exact(const DevCtx c, const int nrows, const double* pos2_given) {
     const int L = c.L, m = c.m;
     const size_t L2 = (size_t)L * L;
@@ -360,34 +410,7 @@ __global__ void k_interp_exact(const DevCtx c, const int nrows, const double* po
                 v[3] = ip_log_exact(w2, KRl + c.iA2[ij], m, v[3]);
             }
             // B1: index_vec.cpp:63-136
-            {
-                const double pos = c.posB1x[i];
-                long long F = (long long)floor(pos);
-                if (F < 1) F = 1; else if (F > maxceil) F = maxceil;
-                const double wt = sub((double)F, pos);
-                const double in3 = mul(wt, wt), in4 = mul(in3, wt);
-                const double2 x0 = c.KR[(size_t)(F - 1) * L + j], x1 = c.KR[(size_t)F * L + j];
-                const double2 d1 = c.dKR[(size_t)F * L + j];
-                if (F < nrows - 1) {
-                    const double2 d2 = c.dKR[(size_t)(F + 1) * L + j];
-                    const double dr = c.dtr[F + 1];
-                    const double e0 = sub(sub(1.0, mul(3.0, in3)), mul(2.0, in4));
-                    const double e1 = add(mul(3.0, in3), mul(2.0, in4));
-                    const double e2 = add(add(wt, mul(2.0, in3)), in4);
-                    const double e3 = add(in3, in4);
-                    v[4] = sub(sub(add(mul(e0, x0.x), mul(e1, x1.x)), mul(e2, d1.x)), dvd(mul(e3, d2.x), dr));
-                    v[5] = sub(sub(add(mul(e0, x0.y), mul(e1, x1.y)), mul(e2, d1.y)), dvd(mul(e3, d2.y), dr));
-                    if (c.logr && x0.y > 0.0 && x1.y > 0.0)  // index_vec.cpp:89-100
-                        v[5] = exp(sub(sub(add(mul(e0, log(x0.y)), mul(e1, log(x1.y))), mul(e2, dvd(d1.y, x0.y))),
-                                       mul(dvd(e3, dr), dvd(d2.y, x1.y))));
-                } else {
-                    const double e0 = sub(1.0, in3), e2 = add(wt, in3);
-                    v[4] = add(sub(mul(e0, x0.x), mul(e2, d1.x)), mul(in3, x1.x));
-                    v[5] = add(sub(mul(e0, x0.y), mul(e2, d1.y)), mul(in3, x1.y));
-                    if (c.logr && x0.y > 0.0 && x1.y > 0.0)  // index_vec.cpp:122-127
-                        v[5] = exp(sub(add(mul(e0, log(x0.y)), mul(in3, log(x1.y))), mul(e2, dvd(d1.y, x0.y))));
-                }
-            }
+            b1_exact(c, nrows, maxceil, i, j, v[4], v[5]);
             // B2: index_mat.cpp:18-91
             {
                 long long X = (long long)pos2;
@@ -739,6 +762,14 @@ cudaError_t launch_interp_exact(const DevCtx& c, int nrows, const double* p1, co
     const int blocks = (int)((L2 + 255) / 256 < 4096 ? (L2 + 255) / 256 : 4096);
     k_interp_exact<<<blocks, 256, 0, st>>>(c, nrows, p2);
     k_rint_exact<<<(c.L + 127) / 128, 128, 0, st>>>(c, nrows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_b1_exact(const DevCtx& c, int nrows, double* qk, double* qr, cudaStream_t st) {
+    k_pos_b1_exact<<<1, 256, 0, st>>>(c, nrows, nullptr, nullptr);
+    const size_t L2 = (size_t)c.L * c.L;
+    const int blocks = (int)((L2 + 255) / 256 < 4096 ? (L2 + 255) / 256 : 4096);
+    k_b1_exact<<<blocks, 256, 0, st>>>(c, nrows, qk, qr);
     return cudaGetLastError();
 }
 

@@ -230,6 +230,8 @@ cudaError_t launch_pos_init(const DevCtx& c, int nrows, cudaStream_t st);
 cudaError_t launch_interp_exact(const DevCtx& c, int nrows, const double* pos1_given,
                                 const double* pos2_given, cudaStream_t st);
 cudaError_t launch_qkr_exact(const DevCtx& c, int nrows, double2* out, cudaStream_t st);
+// posB1x of the state's last time and the reference-order B1 pair of every target
+cudaError_t launch_b1_exact(const DevCtx& c, int nrows, double* qk, double* qr, cudaStream_t st);
 cudaError_t launch_rstep_exact(const DevCtx& c, int nrows, double* out, cudaStream_t st);
 cudaError_t launch_drstep2_exact(const DevCtx& c, const double* qK, const double* qR,
                                  const double* dqK, const double* dqR, double t, double* out,

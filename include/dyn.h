@@ -271,6 +271,44 @@ dyn_status dyn_rollback(void* ctx, int nrows);
  * (what the driver loop reads after each step, simulation_runner.cpp:306-310). */
 dyn_status dyn_last_row(void* ctx, double* qK, double* qR);
 
+/* ------------------------------------------------ device-resident history */
+/* The history in the reference's own device layout (SimulationData's
+ * d_QKv, d_QRv, d_dQKv, d_dQRv: row-major n x len; d_t1grid,
+ * d_delta_t_ratio, d_rvec, d_drvec: n), as device pointers.  For a driver
+ * that keeps its thrust vectors (include/simulation/simulation_data.hpp:12-55)
+ * and hands them to this library: the drop-in layer of RG-Evo's hot-path
+ * symbols exchanges state with RG-Evo through these calls. */
+typedef struct {
+    size_t n;
+    double* t1grid;
+    double* delta_t_ratio;
+    double* QK;
+    double* QR;
+    double* dQK;
+    double* dQR;
+    double* rvec;
+    double* drvec;
+} dyn_state_dev;
+/* Replace the whole history from device arrays (as dyn_state_upload; the
+ * times are checked on the host, the values are not read back). */
+dyn_status dyn_state_upload_dev(void* ctx, const dyn_state_dev* st);
+/* Overwrite rows [row0, row0 + nrows) of the context's history (values,
+ * derivatives, r, dr; not the times) from device arrays indexed like the full
+ * history (row k at offset k * len): for a caller that edited rows in place,
+ * as the reference's tail fit edits the newest row (tail_fit.cu). */
+dyn_status dyn_state_rows_load_dev(void* ctx, size_t row0, size_t nrows, const dyn_state_dev* src);
+/* Copy rows [row0, row0 + nrows) of the context's history, times included,
+ * into device arrays indexed like the full history (appendAllGPU_ptr's
+ * effect, time_steps.cu:766-919, when the caller has grown its arrays). */
+dyn_status dyn_state_rows_store_dev(void* ctx, size_t row0, size_t nrows, const dyn_state_dev* dst);
+/* After dyn_interpolate: materialized array `which` into a device buffer
+ * (the sim->d_*int arrays interpolateGPU fills, interpolation_core.cu:63-159). */
+dyn_status dyn_get_interp_dev(void* ctx, int which, double* dev_out);
+/* The reference-order B1 pair QK_B1, QR_B1 ([len*len] each) of the current
+ * state into device buffers: what RG-Evo's saves read back after a step
+ * (io_save_compressed.cpp:17-63), without the other fourteen arrays. */
+dyn_status dyn_interp_b1_dev(void* ctx, double* qk_b1, double* qr_b1);
+
 /* ----------------------------------------------------------- measurement */
 /* Average device time of the two stage kernels for the current state, timed
  * with CUDA events on the context's stream over `reps` launches. */

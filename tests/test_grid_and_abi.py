@@ -200,7 +200,8 @@ STRUCTS = [("Config", "dyn_config"), ("Tables", "dyn_tables"), ("StateC", "dyn_s
            ("Controller", "dyn_controller"), ("StepResult", "dyn_step_result"), ("RunParams", "dyn_run_params"),
            ("TailInfo", "dyn_tail_info"), ("NoAllocRHS", "dyn_noalloc_rhs"), ("BatchGrid", "dyn_batch_grid"),
            ("BatchQuench", "dyn_batch_quench"), ("BatchConfig", "dyn_batch_config"), ("BatchInfo", "dyn_batch_info"),
-           ("AdjointObjective", "dyn_adjoint_objective"), ("AdjointStats", "dyn_adjoint_stats")]
+           ("AdjointObjective", "dyn_adjoint_objective"), ("AdjointStats", "dyn_adjoint_stats"),
+           ("StateDev", "dyn_state_dev")]
 
 
 def test_ctypes_structs_match_the_header(tmp_path):
