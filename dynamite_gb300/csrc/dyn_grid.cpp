@@ -3,6 +3,14 @@
 // int.dat quadrature weights (integration.cpp:14-195), local barycentric
 // stencils for A1/A2/B2 (interpolation_weights.cpp:12-147, grid_cli.cpp:78-215).
 //
+// Published methods restated here: the knot-span search and the Cox-de Boor
+// basis recurrence of Piegl & Tiller, "The NURBS Book" (algorithms A2.1 and
+// A2.2) for the spline quadrature; barycentric Lagrange interpolation
+// (Berrut & Trefethen, SIAM Review 46, 2004) for the polynomial stencils;
+// Floater & Hormann's rational interpolant (Numer. Math. 107, 2007) for the
+// rational ones; Halley's iteration for the Lambert W_{-1} branch.  The steps
+// follow the reference generator's, so that the tables are bit-identical.
+//
 // Arithmetic is long double like the reference built without Boost
 // (mp_type.hpp), with its transcendental calls in double (see dexp below):
 // on x86-64 long double is the same 80-bit format, so the tables match the

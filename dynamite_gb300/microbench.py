@@ -14,6 +14,8 @@ the staggered derivatives (t_k - t_{k-1}) d/dt C(t, theta_j t) at t_{k-1}
     python -m dynamite_gb300.microbench --form adjoint --L 512 --steps 20
     python -m dynamite_gb300.microbench --form mixed_error --L 1024 --steps 5000
     python -m dynamite_gb300.microbench --form long --L 512 --steps 400000 --tmax 1e6
+    python -m dynamite_gb300.microbench --form decades --L 1024 --tmax 1e7 --wall 1500
+    python -m dynamite_gb300.microbench --form batch_job --tscale 1e-3 --wall 1200
 
 `fp64` / `mixed` time the single-quench gather+convolution kernel and the
 epilogue (one right-hand side at t = t_{n-1}); `batch` times the batched
@@ -28,7 +30,10 @@ C(t, t), and at the final time t_f C(t_f/2, t_f) and R(t_f, t_f/2); `long`
 runs the FP64 form from t=0 to `tmax` (at most `steps` steps) with the
 reference driver's periodic sparsify every 100000 loops, then the mixed
 form on that step schedule, and reports steps, wall times, history sizes and
-the final-time observables of both.
+the final-time observables of both; `decades` runs one quench in the FP64, mixed and
+(hi, lo) forms side by side (the mixed forms on the FP64 schedule, periodic block with the
+SERK2 climb) and reports, at every decade t_d of the run, E(t_d), r(t_d), R(t_d, t_d/2) and
+C(2 t_d, t_d) of each form with the mixed forms' relative errors.
 Prints one JSON line.
 """
 from __future__ import annotations
@@ -131,9 +136,141 @@ def long_run(grid: Grid, nmax: int, tmax: float, T: float = 0.6, lam: float = 0.
     return out
 
 
+def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0.5, every: int = 100000,
+            use_serk2: bool = True, chunk: int = 2000, out_path: str | None = None) -> dict:
+    """One quench in the FP64, mixed and (hi, lo) mixed forms: the FP64 form runs its own
+    controller with the reference GPU loop's periodic block (sparsify every `every` loops,
+    SERK2 climb), the two mixed forms replay its step schedule chunk by chunk with the same
+    cadence (their own sparsify flags).  At every decade t_d = 1, 10, ... up to tmax the run
+    stops at the first step reaching t_d and at the first reaching 2 t_d; per form it records
+    E(t_d) and r(t_d), R(t_d, t_d/2) = QR of the row at t_d evaluated at theta = (t_d/2)/t, and
+    C(2 t_d, t_d) = QK of the row at 2 t_d at theta = t_d/t (a 10-point Lagrange functional of
+    the row, the same on every form); the mixed forms' errors are relative to the FP64 values.
+    Stops early after `wall` seconds; with out_path every finished decade is appended there as
+    one JSON line."""
+    import time
+    from .grid import lagrange_weights
+    from .simulation import Model, Simulation
+    m = Model(p=3, p2=4, lam=lam, Gamma=T)
+    names = ("fp64", "mixed", "mixed_df")
+    sims = {k: Simulation(grid, m, precision=k, history_capacity=4096) for k in names}
+    for s in sims.values():
+        s.init()
+    secs = dict.fromkeys(names, 0.0)
+    steps = 0
+    events = []
+    d = 1.0
+    while d <= tmax:
+        events += [(d, "E", d), (2 * d, "C", d)]
+        d *= 10.0
+    events.sort()
+    rec = {}
+    t_start = time.perf_counter()
+    kw = dict(sparsify_every=every, use_serk2=use_serk2)
+    while events and time.perf_counter() - t_start < wall:
+        target = events[0][0]
+        t0 = time.perf_counter()
+        tr = sims["fp64"].run(chunk, tmax=target, **kw)
+        secs["fp64"] += time.perf_counter() - t0
+        done = int(np.count_nonzero(tr["dt"]))
+        if done == 0:
+            break
+        sched = (tr["dt"][:done], tr["method"][:done])
+        res = {"fp64": tr}
+        for k in names[1:]:
+            t0 = time.perf_counter()
+            res[k] = sims[k].run(done, schedule=sched, **kw)
+            secs[k] += time.perf_counter() - t0
+        steps += done
+        t_now = float(tr["t"][done - 1])
+        while events and t_now >= events[0][0]:
+            _, kind, td = events.pop(0)
+            vals = {}
+            for k in names:
+                qK, qR = sims[k].last_row()
+                if kind == "E":
+                    vals[k] = {"E": float(res[k]["energy"][done - 1]), "r": float(res[k]["r"][done - 1]),
+                               "R_t_thalf": float(lagrange_weights(grid.theta, 0.5 * td / t_now) @ qR)}
+                else:
+                    vals[k] = {"C_2t_t": float(lagrange_weights(grid.theta, td / t_now) @ qK)}
+            e = rec.setdefault(td, {"t": td, "steps_at_t": None, "rows": None})
+            if kind == "E":
+                e.update(steps_at_t=steps, rows={k: sims[k].n for k in names})
+            for k in names:
+                e.setdefault(k, {}).update(vals[k])
+            if kind == "C":
+                for k in names[1:]:
+                    e[k + "_rel_err"] = {q: abs(e[k][q] - e["fp64"][q]) / abs(e["fp64"][q]) for q in e["fp64"]}
+                if out_path:
+                    with open(out_path, "a") as fh:
+                        fh.write(json.dumps(dict(e, seconds=dict(secs), steps=steps)) + "\n")
+    for s in sims.values():
+        s.close()
+    return {"form": "decades", "L": grid.L, "T": T, "lam": lam, "sparsify_every": every, "use_serk2": use_serk2,
+            "steps": steps, "t_reached": t_now if steps else 0.0, "seconds": secs,
+            "steps_per_s": {k: steps / v for k, v in secs.items() if v > 0},
+            "decades": [rec[k] for k in sorted(rec)]}
+
+
+def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool = True, chunk: int = 256,
+              max_gb: float = 150.0) -> dict:
+    """The mixed-L batch run as a whole job: the 64 quenches of mixed_length_quenches (T on
+    [0.4, 1.0], lam 0.3/0.5/0.7, L from {256, 512, 1024} and t_stop log-uniform on
+    [1e4, 1e7], both drawn from mt19937_64) with every t_stop multiplied by `tscale`, the
+    periodic block of the reference GPU loop (sparsify every `every` loops, SERK2 climb) and
+    the gather tile the autotuner picks after the first ticks; run until every quench has
+    stopped (or `wall` seconds).  History capacity per quench from the step count a quench
+    needs to reach its t_stop (about 424 t^0.577 steps for the mixed p-spin at T = 0.6, with
+    a 1.5 margin); the job is refused above `max_gb` of history memory."""
+    import time
+    from . import grid as G
+    from .batch import Batch, mixed_length_quenches
+    lengths, qs = mixed_length_quenches(n=64)
+    need = 0.0
+    for q in qs:
+        q.t_stop *= tscale
+        q.capacity = int(1.5 * 424.0 * q.t_stop ** 0.577) + 2048
+        need += q.capacity * lengths[q.grid] * 48.0  # FP64 (QK, QR), (dQK, dQR) + their FP32 mirrors
+    if need / 1e9 > max_gb:
+        raise ValueError(f"batch job needs {need / 1e9:.0f} GB of history, above {max_gb} GB: lower tscale")
+    grids = [G.generate(L) for L in lengths]
+    bt = Batch(grids, qs, ticks_per_launch=32, sparsify_every=every, use_serk2=use_serk2)
+    t0 = time.perf_counter()
+    ticks = bt.run(512)
+    tile = bt.tune(reps=3)
+    while time.perf_counter() - t0 < wall:
+        k = bt.run(chunk * 32)
+        ticks += k
+        if k < chunk * 32:
+            break
+    sec = time.perf_counter() - t0
+    infos = bt.infos()
+    bt.close()
+    per_L = {}
+    for q, i in zip(qs, infos):
+        d = per_L.setdefault(str(lengths[q.grid]), {"quenches": 0, "steps": 0})
+        d["quenches"] += 1
+        d["steps"] += i["steps"]
+    total = sum(i["steps"] for i in infos)
+    status = {}
+    for i in infos:
+        status[i["status"]] = status.get(i["status"], 0) + 1
+    reached = [i["t"] / q.t_stop for q, i in zip(qs, infos)]
+    return {"form": "batch_job", "quenches": len(qs), "tscale": tscale,
+            "t_stop_range": [min(q.t_stop for q in qs), max(q.t_stop for q in qs)], "sparsify_every": every,
+            "use_serk2": use_serk2, "tile": tile, "ticks": ticks, "seconds": sec, "rk_steps": total,
+            "steps_per_s": total / sec, "per_L": per_L, "status": status,
+            "t_over_t_stop_range": [min(reached), max(reached)], "history_gb": need / 1e9,
+            "max_rows": max(i["n"] for i in infos)}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error", "long"], default="batch")
+    ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error", "long", "decades", "batch_job"],
+                    default="batch")
+    ap.add_argument("--wall", type=float, default=600.0, help="decades / batch_job: stop after this many seconds")
+    ap.add_argument("--tscale", type=float, default=1e-3, help="batch_job: factor on every stopping time")
+    ap.add_argument("--out", default=None, help="decades: append each finished decade to this file")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--tune", action="store_true", help="batch: autotune the gather tile first")
     ap.add_argument("--tmax", type=float, default=0.0, help="mixed_error: run the FP64 form to t >= tmax")
@@ -161,6 +298,12 @@ def main(argv=None):
         s.close()
         print(json.dumps({"form": "adjoint", "L": a.L, "steps": a.steps, "t_final": float(fw["t"][-1]),
                           "dE_dT": float(g[0]), "dE_dlam": float(g[1]), **stats}))
+        return
+    if a.form == "batch_job":
+        print(json.dumps(batch_job(a.tscale, a.wall)))
+        return
+    if a.form == "decades":
+        print(json.dumps(decades(grid, a.tmax, a.wall, a.T, out_path=a.out)))
         return
     if a.form == "long":
         print(json.dumps(long_run(grid, a.steps, a.tmax, a.T, precision=a.precision)))
