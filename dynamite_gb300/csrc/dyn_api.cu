@@ -813,10 +813,21 @@ dyn_status dyn_ctx_create(const dyn_config* cfg, const dyn_tables* tb, void** ou
         float2 *f1, *f2, *f3;
         if ((s = dalloc(&f1, planes * L2)) || (s = dalloc(&f2, planes * L2)) || (s = dalloc(&f3, planes * L2))) { delete c; return s; }
         d.wA1f = f1; d.wA2f = f2; d.wB2f = f3;
-        float* itf;
-        if ((s = dalloc(&itf, L))) { delete c; return s; }
+        float* itf;  // [2L]: int.dat as FP32 (hi, lo) planes
+        if ((s = dalloc(&itf, 2 * L))) { delete c; return s; }
         d.integ_f = itf;
-        if (launch_weights_f32(it, itf, L, c->st) != cudaSuccess) { delete c; return fail(DYN_ERR_CUDA, "FP32 int.dat copy failed"); }
+        d.integ_l = itf + L;
+        {
+            std::vector<float> hl(2 * L);
+            for (size_t k = 0; k < L; ++k) {
+                hl[k] = (float)tb->integ[k];
+                hl[L + k] = (float)(tb->integ[k] - (double)hl[k]);
+            }
+            if (cudaMemcpy(itf, hl.data(), 2 * L * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+                delete c;
+                return fail(DYN_ERR_CUDA, "FP32 int.dat copy failed");
+            }
+        }
         if (launch_weights_tapmajor(w1, f1, L2, (int)m, c->st) != cudaSuccess ||
             launch_weights_tapmajor(w2, f2, L2, (int)m, c->st) != cudaSuccess ||
             launch_weights_tapmajor(w3, f3, L2, (int)m, c->st) != cudaSuccess || cudaStreamSynchronize(c->st) != cudaSuccess) {

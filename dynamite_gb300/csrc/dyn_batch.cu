@@ -248,12 +248,12 @@ __device__ void adapt_step(const Quench& q, Plan& pl, const TabDev& tb) {
 #define DYN_BATCH_SHIFT 0
 #endif
 #ifndef DYN_BATCH_DF_TPSM
-#define DYN_BATCH_DF_TPSM 1152
+#define DYN_BATCH_DF_TPSM 1024
 #endif
-// DF: the (hi, lo) form (mdf::chunk): twice the staged row; its cap of 56
-// registers (DYN_BATCH_DF_TPSM = 1152 threads per SM) spills but beats 128
-// registers at 512 threads: 1.53 vs 1.80 ms for 64 quenches at L=512 (64
-// registers: 1.57, 72: 1.64, 48: 1.77).
+// DF: the (hi, lo) form (mdf::chunk_dd): twice the staged row and a double-float
+// tail; a cap of 64 registers (DYN_BATCH_DF_TPSM = 1024 threads per SM) spills a
+// little but measured best for 64 quenches at L=512: 1.92 ms against 2.02 (56
+// registers), 1.98 (72) and 2.15 (80).
 template <int M, int K, int P, int P2, int TPB, bool DF = false>
 __global__ void __launch_bounds__(TPB, DF ? DYN_BATCH_DF_TPSM / TPB : (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
     k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(TPB, DF ? DYN_BATCH_DF_TPSM / TPB : (K == 1 ? 
             for (int ch0 = 0; ch0 < nch; ch0 += GMAX) {
                 const int ng = min(GMAX, nch - ch0);
                 for (int g = 0; g < ng; ++g) {
-                    if constexpr (DF) mdf::chunk<M, K, P, P2>(q.c, sp, ch0 + g, g, s_lastf, s_lo, s_clo, sh, i);
+                    if constexpr (DF) mdf::chunk_dd<M, K, P, P2>(q.c, sp, ch0 + g, g, s_lastf, s_lo, s_clo, sh, i);
                     else mixed::chunk_sums<M, K, P, P2, DYN_BATCH_SHIFT>(q.c, sp, ch0 + g, g, s_lastf, sh, i);
                 }
                 __syncthreads();
@@ -758,9 +758,12 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         if (!check_tables(L, m, &grids[g].tables, i32, why)) { delete bt; return bfail(DYN_ERR_INVALID, why); }
         const dyn_tables& tb = grids[g].tables;
         if ((s = bt->alloc(&gd.theta, L)) || (s = bt->alloc(&gd.phi2, L2)) || (s = bt->alloc(&gd.integ, L)) ||
-            (s = bt->alloc(&gd.integ_f, L))) { delete bt; return s; }
-        std::vector<float> f(L);
-        for (size_t k = 0; k < L; ++k) f[k] = (float)tb.integ[k];
+            (s = bt->alloc(&gd.integ_f, 2 * L))) { delete bt; return s; }
+        std::vector<float> f(2 * L);  // int.dat as FP32 (hi, lo) planes
+        for (size_t k = 0; k < L; ++k) {
+            f[k] = (float)tb.integ[k];
+            f[L + k] = (float)(tb.integ[k] - (double)f[k]);
+        }
 #define BUP(dst, src, bytes)                                                                       \
     if ((e = cudaMemcpy((void*)(dst), (src), (bytes), cudaMemcpyHostToDevice)) != cudaSuccess) {  \
         delete bt;                                                                                 \
@@ -769,7 +772,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         BUP(gd.theta, tb.theta, L * sizeof(double));
         BUP(gd.phi2, tb.phi2, L2 * sizeof(double));
         BUP(gd.integ, tb.integ, L * sizeof(double));
-        BUP(gd.integ_f, f.data(), L * sizeof(float));
+        BUP(gd.integ_f, f.data(), 2 * L * sizeof(float));
         const double* w[3] = {tb.weightsA1y, tb.weightsA2y, tb.weightsB2y};
         const size_t planes = (m + 1) / 2;
         std::vector<float2> wt(planes * L2);
@@ -842,6 +845,7 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
         d.phi2 = gd.phi2;
         d.integ = gd.integ;
         d.integ_f = gd.integ_f;
+        d.integ_l = gd.integ_f + gd.L;
         d.iA1 = gd.iA[0];
         d.iA2 = gd.iA[1];
         d.iB2 = gd.iA[2];

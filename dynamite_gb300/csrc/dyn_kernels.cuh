@@ -106,6 +106,7 @@ struct DevCtx {
     const float2* wA2l;
     const float2* wB2l;
     const float* integ_f;  // [L]   int.dat in FP32
+    const float* integ_l;  // [L]   its low parts, int.dat - (double)integ_f (mixed forms)
     float* inv_dtr_f;      // [cap] 1/delta_t_ratio in FP32
     float* inv_len_f;      // [cap] 1/(t1grid[k+1]-t1grid[k]) in FP32
     // materialized interpolation (dyn_interpolate)
@@ -258,7 +259,6 @@ cudaError_t launch_mirror_lo(const double2* in, float2* out, size_t count, cudaS
 // shortened or replaced history leaves behind (they may hold a failed step's NaN).
 cudaError_t clear_mirror_rows(const DevCtx& c, size_t r0, size_t r1, cudaStream_t st);
 cudaError_t launch_weights_tapmajor_lo(const double* in, float2* out, size_t targets, int m, cudaStream_t st);
-cudaError_t launch_weights_f32(const double* in, float* out, size_t count, cudaStream_t st);
 // [L*L][m] FP64 stencil rows to the tap-major FP32 pair planes of the mixed form
 cudaError_t launch_weights_tapmajor(const double* in, float2* out, size_t targets, int m, cudaStream_t st);
 cudaError_t launch_time_f32(const double* t1, const double* dtr, int n, float* inv_len, float* inv_dtr,

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(128, K == 1 ? 8 : 4) k_main_df(const DevCtx c,
     mixed::row_setup(c, sp, i, blockIdx.x == 0, s_row, sh, s_clo);
     mdf::stage_lo(c, sp, s_lo);
     __syncthreads();
-    mdf::chunk<M, K, P, P2>(c, sp, blockIdx.x, 0, s_row, s_lo, s_clo, sh, i);
+    mdf::chunk_dd<M, K, P, P2>(c, sp, blockIdx.x, 0, s_row, s_lo, s_clo, sh, i);
     __syncthreads();
     mixed::fold_chunks(c, i, gridDim.x, blockIdx.x, 1, sh);
 }
@@ -109,11 +109,6 @@ __global__ void k_time_f32(const double* t1, const double* dtr, int n, float* in
     }
 }
 
-__global__ void k_weights_f32(const double* in, float* out, size_t count) {
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
-        out[e] = (float)in[e];
-}
-
 // out[p][e] = (w[e][2p], w[e][2p+1]) in FP32 (second tap 0 past the depth);
 // with LO the low parts w - (double)(float)w instead
 template <bool LO>
@@ -170,12 +165,6 @@ cudaError_t launch_weights_tapmajor_lo(const double* in, float2* out, size_t tar
 cudaError_t launch_mirror_lo(const double2* in, float2* out, size_t count, cudaStream_t st) {
     const int blocks = (int)((count + 255) / 256 < 8192 ? (count + 255) / 256 : 8192);
     k_to_f32_lo<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, count);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_weights_f32(const double* in, float* out, size_t count, cudaStream_t st) {
-    const int blocks = (int)((count + 255) / 256 < 8192 ? (count + 255) / 256 : 8192);
-    k_weights_f32<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in, out, count);
     return cudaGetLastError();
 }
 

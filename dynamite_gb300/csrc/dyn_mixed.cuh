@@ -175,18 +175,19 @@ __device__ __forceinline__ void load_w10(const float2* __restrict__ w, size_t L2
 }
 
 // TwoSum accumulation: s + c carries the sum to about twice FP32 precision
+// (round-to-nearest intrinsics: a product passed as v is never fused into the sum)
 __device__ __forceinline__ void two_sum_add(float& s, float& c, float v) {
-    const float t = s + v;
-    const float bp = t - s;
-    c += (s - (t - bp)) + (v - bp);
+    const float t = __fadd_rn(s, v);
+    const float bp = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(v, bp)));
     s = t;
 }
 
 // (hi, lo) += (h2, l2) with TwoSum on the high parts
 __device__ __forceinline__ void pair_add(float& h, float& l, float h2, float l2) {
-    const float t = h + h2;
-    const float bp = t - h;
-    l = l + l2 + ((h - (t - bp)) + (h2 - bp));
+    const float t = __fadd_rn(h, h2);
+    const float bp = __fsub_rn(t, h);
+    l = __fadd_rn(__fadd_rn(l, l2), __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(h2, bp)));
     h = t;
 }
 
@@ -489,21 +490,23 @@ __device__ __forceinline__ void fold_chunks(const DevCtx& c, const int i, const 
 // sums over them).  Here the weights and the stored (QK, QR) history carry FP32
 // (hi, lo) pairs; the A1/A2 and B2 stencil sums form every term as an exact
 // FP32 product plus the cross terms (w_hi x_lo + w_lo x_hi) and add them with
-// TwoSum; each gathered value is rounded once to FP32 for Sigma and the
-// convolution products.  B1 combines old rows with coefficients that move with
-// t: plain products with the low parts as cross terms suffice there.  The
-// derivative rows (dQK, dQR), a step's worth of change, stay single FP32.
+// TwoSum; the gathered values stay (hi, lo) and everything that changes from
+// stage to stage -- the B2 interval offset, the Hermite weights, B1, Sigma and
+// the eight int.dat products -- runs in double-float (chunk_dd), so the stage
+// derivatives carry no stage-to-stage FP32 rounding noise and the embedded error
+// estimate sees the method's error, as in the FP64 form.  The derivative rows
+// (dQK, dQR), a step's worth of change, stay single FP32.
 namespace mdf {
 using namespace mixed;
 
 // (s, c) += (wh + wl) * (xh + xl)
 __device__ __forceinline__ void add_prod(float& s, float& c, float wh, float wl, float xh, float xl) {
-    const float p = wh * xh;
-    float e = fmaf(wh, xh, -p);
-    e = fmaf(wh, xl, e);
-    e = fmaf(wl, xh, e);
-    const float t = s + p, bp = t - s;
-    c += ((s - (t - bp)) + (p - bp)) + e;
+    const float p = __fmul_rn(wh, xh);  // intrinsics: no fusing of the product into the sums
+    float e = __fmaf_rn(wh, xh, -p);
+    e = __fmaf_rn(wh, xl, e);
+    e = __fmaf_rn(wl, xh, e);
+    const float t = __fadd_rn(s, p), bp = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp)), e));
     s = t;
 }
 
@@ -578,24 +581,99 @@ __device__ __forceinline__ void load_w10_hl(const float2* __restrict__ wh, const
     }
 }
 
-// One chunk of tpb*K targets of row i in the (hi, lo) form (as chunk_sums);
-// s_hi / s_lo: the staged last row, clo: low parts of the B1 coefficients.
+// ---- double-float arithmetic: an unevaluated sum h + l of two floats, ~44 bits.
+// Every operation is a round-to-nearest intrinsic, so the compiler never fuses a
+// product into a following sum (which would break the error-free transformations
+// and make the result depend on how a kernel was inlined).
+struct ff {
+    float h, l;
+};
+__device__ __forceinline__ ff ff_split(double v) {
+    const float h = __double2float_rn(v);
+    return {h, __double2float_rn(__dsub_rn(v, (double)h))};
+}
+__device__ __forceinline__ ff ff_fast(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const float s = __fadd_rn(a.h, b.h), bp = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bp)), __fsub_rn(b.h, bp)), __fadd_rn(a.l, b.l));
+    return ff_fast(s, e);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return ff_fast(p, e);
+}
+__device__ __forceinline__ ff ff_mulf(ff a, float b) {
+    const float p = __fmul_rn(a.h, b);
+    float e = __fmaf_rn(a.h, b, -p);
+    e = __fmaf_rn(a.l, b, e);
+    return ff_fast(p, e);
+}
+// q^E as the same left-to-right product chain whether E is a template constant
+// (the specialized models) or a run-time value (the generic kernel): both forms
+// round alike, so a quench gives the same result in either kernel
+template <int E>
+__device__ __forceinline__ ff ff_pow_c(ff q) {
+    if constexpr (E <= 0) {
+        return {1.f, 0.f};
+    } else {
+        ff r = q;
+#pragma unroll
+        for (int k = 1; k < E; ++k) r = ff_mul(r, q);
+        return r;
+    }
+}
+__device__ __forceinline__ ff ff_pow_r(ff q, int e) {
+    if (e <= 0) return {1.f, 0.f};
+    ff r = q;
+    for (int k = 1; k < e; ++k) r = ff_mul(r, q);
+    return r;
+}
+struct FFModel {
+    int p, p2;
+    ff cA, cB, cC, cD;
+};
+// f'(q) and f''(q) in double-float
+template <int P, int P2>
+__device__ __forceinline__ void ff_sigma(const FFModel& M, ff q, ff& d1, ff& d2) {
+    if constexpr (P >= 0) {
+        d1 = ff_add(ff_mul(M.cA, ff_pow_c<P - 1>(q)), ff_mul(M.cB, ff_pow_c<P2 - 1>(q)));
+        d2 = ff_add(ff_mul(M.cC, ff_pow_c<P - 2>(q)), ff_mul(M.cD, ff_pow_c<P2 - 2>(q)));
+    } else {
+        d1 = ff_add(ff_mul(M.cA, ff_pow_r(q, M.p - 1)), ff_mul(M.cB, ff_pow_r(q, M.p2 - 1)));
+        d2 = ff_add(ff_mul(M.cC, ff_pow_r(q, M.p - 2)), ff_mul(M.cD, ff_pow_r(q, M.p2 - 2)));
+    }
+}
+
+// chunk with everything that changes from stage to stage in double-float: the B2
+// interval offset (one FP64 residual), the Hermite weights, the gathered values
+// (the compensated sums kept as (hi, lo)), Sigma and the eight int.dat products,
+// accumulated as (hi, lo) pairs.  FP32 roundings that differ between the stages of
+// one step would otherwise put a noise of ~1e-7 of |h| into every stage derivative,
+// which the embedded error estimate sees: with delta_max = 1e-10 the controller
+// then keeps the step ~1000x below the FP64 form's.  The roundings of the frozen
+// inputs (the (hi, lo) weights and history, the FP32 derivative rows) vary smoothly
+// with the stage time and cancel in the estimate.
 template <int M, int K, int P, int P2>
-__device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const int ch, const int slot,
-                                      const float2* s_hi, const float2* s_lo, const float* clo, RowShared& sh,
-                                      const int i) {
+__device__ __forceinline__ void chunk_dd(const DevCtx& c, const StageDev& sp, const int ch, const int slot,
+                                         const float2* s_hi, const float2* s_lo, const float* clo, RowShared& sh,
+                                         const int i) {
     const int L = c.L, tpb = blockDim.x;
     const size_t L2 = (size_t)L * L;
     const int nrows = sp.nrows;
     const double t = sp.T;
     const bool live = t > 0.0;
-    const FModel Mf{c.M.p, c.M.p2, (float)c.M.cA, (float)c.M.cB, (float)c.M.cC, (float)c.M.cD};
+    const FFModel Mf{c.M.p, c.M.p2, ff_split(c.M.cA), ff_split(c.M.cB), ff_split(c.M.cC), ff_split(c.M.cD)};
     const int m = M > 0 ? M : c.m;
-    const float bh0 = sh.c[0], bh1 = sh.c[1], bh2 = sh.c[2], bh3 = sh.c[3];
-    const float bl0 = clo[0], bl1 = clo[1];
+    const ff bc0{sh.c[0], clo[0]}, bc1{sh.c[1], clo[1]}, bc2{sh.c[2], clo[2]}, bc3{sh.c[3], clo[3]};
     const int F = sh.bi[0], cubic1 = sh.bi[1];
     const int maxX = sp.maxX;
-    const float2 fill = c.KRf[0];
     const ListView lv{c.t1grid, nrows, t};
     float acc[8], cmp[8];
 #pragma unroll
@@ -605,7 +683,7 @@ __device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const
         const int j = ch * tpb * K + kk * tpb + threadIdx.x;
         if (j < L) {
             const size_t ij = (size_t)i * L + j;
-            float2 a1, a2, b1, b2;
+            ff a1x, a1y, a2x, a2y, b1x, b1y, b2x, b2y;
             if (live) {
                 {
                     const int s1 = __ldg(c.iA1 + ij), s2 = __ldg(c.iA2 + ij);
@@ -620,30 +698,42 @@ __device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const
                         g1 = gather<M>(c.wA1f, c.wA1l, L2, ij, s_hi + s1, s_lo + s1, m, false);
                         g2 = gather<M>(c.wA2f, c.wA2l, L2, ij, s_hi + s2, s_lo + s2, m, false);
                     }
-                    a1 = make_float2(g1.x + g1.y, g1.z + g1.w);
-                    a2 = make_float2(g2.x + g2.y, g2.z + g2.w);
+                    a1x = ff_fast(g1.x, g1.y);
+                    a1y = ff_fast(g1.z, g1.w);
+                    a2x = ff_fast(g2.x, g2.y);
+                    a2y = ff_fast(g2.z, g2.w);
                 }
                 {
                     const size_t r0 = (size_t)(F - 1) * L + j, r1 = (size_t)F * L + j;
                     const float2 x0 = __ldg(c.KRf + r0), x0l = __ldg(c.KRl + r0);
                     const float2 x1 = __ldg(c.KRf + r1), x1l = __ldg(c.KRl + r1);
                     const float2 d1 = __ldg(c.dKRf + r1);
-                    // the coefficients move with t, so plain FP32 products suffice once the
-                    // rows' low parts and c0, c1's low parts enter as cross terms
                     const float2 d2 = cubic1 ? __ldg(c.dKRf + (size_t)(F + 1) * L + j) : make_float2(0.f, 0.f);
-                    b1.x = bh0 * x0.x + (bl0 * x0.x + bh0 * x0l.x + bh1 * x1l.x + bl1 * x1.x - bh2 * d1.x - bh3 * d2.x) +
-                           bh1 * x1.x;
-                    b1.y = bh0 * x0.y + (bl0 * x0.y + bh0 * x0l.y + bh1 * x1l.y + bl1 * x1.y - bh2 * d1.y - bh3 * d2.y) +
-                           bh1 * x1.y;
+                    const ff dx = ff_add(ff_mulf(bc2, d1.x), ff_mulf(bc3, d2.x));
+                    const ff dy = ff_add(ff_mulf(bc2, d1.y), ff_mulf(bc3, d2.y));
+                    b1x = ff_add(ff_add(ff_mul(bc0, ff{x0.x, x0l.x}), ff_mul(bc1, ff{x1.x, x1l.x})), ff_neg(dx));
+                    b1y = ff_add(ff_add(ff_mul(bc0, ff{x0.y, x0l.y}), ff_mul(bc1, ff{x1.y, x1l.y})), ff_neg(dy));
                 }
                 {
-                    int X;
-                    float x;
                     const double El = __dmul_rn(__ldg(c.phi2 + ij), t);
-                    split_at(lv, c.inv_len_f, El, floor_index(lv, El, sh.seg[j >> 5], sh.seg[(j >> 5) + 1]), X, x);
-                    if (X > maxX) { x += __int2float_rn(X - maxX); X = maxX; }
-                    if (X < 1) { x -= __int2float_rn(1 - X); X = 1; }
-                    const float x2 = x * x, x3 = x2 * x;
+                    const int k = floor_index(lv, El, sh.seg[j >> 5], sh.seg[(j >> 5) + 1]);
+                    // offset in the interval: x = (El - t_k) / (t_{k+1} - t_k) as x_h + x_l, x_h
+                    // from the FP32 inverse length, x_l from the FP64 residual
+                    int X;
+                    ff x{0.f, 0.f};
+                    if (k >= lv.n - 1) {
+                        X = lv.n;
+                    } else {
+                        const double lo = lv.at(k), diff = __dsub_rn(El, lo), len = __dsub_rn(lv.at(k + 1), lo);
+                        const float il = __ldg(c.inv_len_f + k);
+                        const float xh = __fmul_rn(__double2float_rn(diff), il);
+                        x = ff{xh, __fmul_rn(__double2float_rn(__fma_rn(-(double)xh, len, diff)), il)};
+                        X = k + 1;
+                        if (x.h >= 1.0f) { X = k + 2; x = ff_add(x, ff{-1.f, 0.f}); }
+                    }
+                    if (X > maxX) { x = ff_add(x, ff{__int2float_rn(X - maxX), 0.f}); X = maxX; }
+                    if (X < 1) { x = ff_add(x, ff{-__int2float_rn(1 - X), 0.f}); X = 1; }
+                    const ff x2 = ff_mul(x, x), x3 = ff_mul(x2, x);
                     const size_t base = (size_t)(X - 1) * (size_t)L + (size_t)__ldg(c.iB2 + ij);
                     const bool cubic2 = X < nrows - 1;
                     float4 S0, S1;
@@ -662,41 +752,44 @@ __device__ __forceinline__ void chunk(const DevCtx& c, const StageDev& sp, const
                         D1 = dotfT(c.wB2f, L2, ij, c.dKRf + base + L, m, true);
                         if (cubic2) D2 = dotfT(c.wB2f, L2, ij, c.dKRf + base + 2 * L, m, true);
                     }
-                    // S0 + e2 (S1 - S0) + e1 D1 + e3 D2 (e0 = 1 - e2): the FP32 Hermite
-                    // weights only scale the row difference
-                    float e1, e2, e3;
+                    // S0 + e2 (S1 - S0) + e1 D1 + e3 D2 (e0 = 1 - e2)
+                    ff e1, e2, e3{0.f, 0.f};
                     if (cubic2) {
-                        e1 = x - 2.f * x2 + x3;
-                        e2 = 3.f * x2 - 2.f * x3;
-                        e3 = (x3 - x2) * __ldg(c.inv_dtr_f + X + 1);
+                        e1 = ff_add(ff_add(x, ff_mulf(x2, -2.f)), x3);
+                        e2 = ff_add(ff_mulf(x2, 3.f), ff_mulf(x3, -2.f));
+                        e3 = ff_mul(ff_add(x3, ff_neg(x2)), ff_split(c.inv_dtr[X + 1]));
                     } else {
-                        e1 = x - x2;
+                        e1 = ff_add(x, ff_neg(x2));
                         e2 = x2;
-                        e3 = 0.f;
                     }
-                    const float dSx = (S1.x - S0.x) + (S1.y - S0.y), dSy = (S1.z - S0.z) + (S1.w - S0.w);
-                    b2.x = S0.x + (S0.y + (e2 * dSx + e1 * D1.x + e3 * D2.x));
-                    b2.y = S0.z + (S0.w + (e2 * dSy + e1 * D1.y + e3 * D2.y));
+                    const ff dSx = ff_add(ff{S1.x, S1.y}, ff{-S0.x, -S0.y});
+                    const ff dSy = ff_add(ff{S1.z, S1.w}, ff{-S0.z, -S0.w});
+                    b2x = ff_add(ff_fast(S0.x, S0.y),
+                                 ff_add(ff_mul(e2, dSx), ff_add(ff_mulf(e1, D1.x), ff_mulf(e3, D2.x))));
+                    b2y = ff_add(ff_fast(S0.z, S0.w),
+                                 ff_add(ff_mul(e2, dSy), ff_add(ff_mulf(e1, D1.y), ff_mulf(e3, D2.y))));
                 }
             } else {
-                a1 = a2 = b1 = b2 = fill;
+                const double2 f0 = c.KR[0];
+                a1x = a2x = b1x = b2x = ff_split(f0.x);
+                a1y = a2y = b1y = b2y = ff_split(f0.y);
             }
-            float sKA1, dA1, sKB1, dB1, sKB2, dB2;
-            SigF<P, P2>::d12(Mf, a1.x, sKA1, dA1);
-            const float sRA1 = dA1 * a1.y;
-            const float sRA2 = SigF<P, P2>::d2(Mf, a2.x) * a2.y;
-            SigF<P, P2>::d12(Mf, b1.x, sKB1, dB1);
-            const float sRB1 = dB1 * b1.y;
-            SigF<P, P2>::d12(Mf, b2.x, sKB2, dB2);
-            const float sRB2 = dB2 * b2.y;
-            const float wj = __ldg(c.integ_f + j);
-            const float wRA2 = wj * sRA2, wQRA2 = wj * a2.y;
-            const float v[8] = {wRA2 * b2.x, (wj * sRA1) * b1.x, (wj * sKA1) * b1.y, wQRA2 * sKB2,
-                                (wj * a1.y) * sKB1, (wj * a1.x) * sRB1, wRA2 * b2.y, wQRA2 * sRB2};
+            ff sKA1, dA1, sKA2, dA2, sKB1, dB1, sKB2, dB2;
+            ff_sigma<P, P2>(Mf, a1x, sKA1, dA1);
+            ff_sigma<P, P2>(Mf, a2x, sKA2, dA2);
+            ff_sigma<P, P2>(Mf, b1x, sKB1, dB1);
+            ff_sigma<P, P2>(Mf, b2x, sKB2, dB2);
+            const ff sRA1 = ff_mul(dA1, a1y), sRA2 = ff_mul(dA2, a2y);
+            const ff sRB1 = ff_mul(dB1, b1y), sRB2 = ff_mul(dB2, b2y);
+            const ff wj{__ldg(c.integ_f + j), __ldg(c.integ_l + j)};
+            const ff wRA2 = ff_mul(wj, sRA2), wQRA2 = ff_mul(wj, a2y);
+            const ff v[8] = {ff_mul(wRA2, b2x),           ff_mul(ff_mul(wj, sRA1), b1x), ff_mul(ff_mul(wj, sKA1), b1y),
+                             ff_mul(wQRA2, sKB2),         ff_mul(ff_mul(wj, a1y), sKB1), ff_mul(ff_mul(wj, a1x), sRB1),
+                             ff_mul(wRA2, b2y),           ff_mul(wQRA2, sRB2)};
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                if (kk == 0) acc[k] = v[k];
-                else two_sum_add(acc[k], cmp[k], v[k]);
+            for (int q = 0; q < 8; ++q) {
+                if (kk == 0) { acc[q] = v[q].h; cmp[q] = v[q].l; }
+                else pair_add(acc[q], cmp[q], v[q].h, v[q].l);
             }
         }
     }

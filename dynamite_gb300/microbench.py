@@ -165,12 +165,21 @@ def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0
         d *= 10.0
     events.sort()
     rec = {}
+    t_now = 0.0
     t_start = time.perf_counter()
     kw = dict(sparsify_every=every, use_serk2=use_serk2)
-    while events and time.perf_counter() - t_start < wall:
+    from ._lib import DYN_ERR_NONFINITE, DynError
+    stopped = None
+    while events and time.perf_counter() - t_start < wall and stopped is None:
         target = events[0][0]
         t0 = time.perf_counter()
-        tr = sims["fp64"].run(chunk, tmax=target, **kw)
+        try:
+            tr = sims["fp64"].run(chunk, tmax=target, **kw)
+        except DynError as e:
+            if e.status != DYN_ERR_NONFINITE:
+                raise
+            stopped = {"form": "fp64", "near_step": steps}
+            break
         secs["fp64"] += time.perf_counter() - t0
         done = int(np.count_nonzero(tr["dt"]))
         if done == 0:
@@ -179,8 +188,15 @@ def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0
         res = {"fp64": tr}
         for k in names[1:]:
             t0 = time.perf_counter()
-            res[k] = sims[k].run(done, schedule=sched, **kw)
+            try:
+                res[k] = sims[k].run(done, schedule=sched, **kw)
+            except DynError as e:
+                if e.status != DYN_ERR_NONFINITE:
+                    raise
+                stopped = {"form": k, "near_step": steps}
             secs[k] += time.perf_counter() - t0
+        if stopped is not None:
+            break
         steps += done
         t_now = float(tr["t"][done - 1])
         while events and t_now >= events[0][0]:
@@ -207,7 +223,7 @@ def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0
     for s in sims.values():
         s.close()
     return {"form": "decades", "L": grid.L, "T": T, "lam": lam, "sparsify_every": every, "use_serk2": use_serk2,
-            "steps": steps, "t_reached": t_now if steps else 0.0, "seconds": secs,
+            "steps": steps, "t_reached": t_now if steps else 0.0, "seconds": secs, "nonfinite": stopped,
             "steps_per_s": {k: steps / v for k, v in secs.items() if v > 0},
             "decades": [rec[k] for k in sorted(rec)]}
 
