@@ -1,7 +1,10 @@
 #!/usr/bin/env python
 """RK steps/s of the DYNAMITE per-step hot path on GB300.
 
-Headline (`value`): the mixed-precision batched form at L=512 -- 64 quenches
+Headline (`value`): the batched (hi, lo) mixed-precision form at L=512 (FP32
+(hi, lo) weights and history, compensated gathers, double-float stage arithmetic,
+FP64 r(t), t, C(t, t) and error norm: its step-size controller takes the FP64
+form's steps) -- 64 quenches
 of the mixed p-spin model f(q)=(1-lam)q^3+lam q^4 (-p 3 -q 4) with
 temperatures uniform on [0.4, 1.0] and lam cycling through 0.3/0.5/0.7, from
 infinite temperature, on one poly-9 grid (Tmax=1e5, spline order 5,
@@ -11,9 +14,11 @@ timed, a tick being one RK stage of every running quench (RK54 / SSPRK(10,4)
 as each quench's controller chooses); value = RK steps completed / time.
 
 Beside it, on the same grid: the plain FP64 form of one quench (lam=0.5,
-T=0.6) after the same setup, its stage kernels and FP64 roofline; the
-single-quench mixed form on that state; the reference CPU path (oracle/
-restatement) on the host cores.  Then the mixed-L batch (64 quenches with
+T=0.6) after the same setup, its stage kernels and FP64 roofline; the batch in
+the plain FP32 mixed form (`--precision mixed` makes it the headline; its
+free controller is held back by FP32 rounding noise, so its steps are far
+smaller than FP64's); the single-quench plain mixed form on the FP64 state; the
+reference CPU path (oracle/ restatement) on the host cores.  Then the mixed-L batch (64 quenches with
 grid lengths from {256, 512, 1024} and stopping times log-uniform on
 [1e4, 1e7]) and the FP64 adjoint (L=512, lam=0.5, T=0.6, 5000 steps:
 gradients of E, C(t, t/2) and r in T and lam against central differences,
@@ -63,7 +68,11 @@ def parse():
     ap.add_argument("--mixed-length-setup", type=int, default=1000,
                     help="untimed steps of every quench of the mixed-L batch before its timed ticks (0: skip it)")
     ap.add_argument("--adjoint-steps", type=int, default=5000, help="FP64 steps of the adjoint measurement (0: skip)")
-    ap.add_argument("--no-df", dest="df", action="store_false", help="skip the batched (hi, lo) form")
+    ap.add_argument("--precision", choices=["mixed_df", "mixed"], default="mixed_df",
+                    help="the headline batch's form: mixed_df, the (hi, lo) form whose step-size controller "
+                         "tracks the FP64 form's (default), or mixed, the plain FP32 form")
+    ap.add_argument("--no-other", dest="other", action="store_false",
+                    help="skip the batch in the other mixed form")
     return ap.parse_args()
 
 
@@ -328,21 +337,23 @@ def _mixed_single(D, torch, args, grid, dev, stream, flush, cap, start):
             "stage_ms": {"main": mm, "epilogue": me}}
 
 
-def _batch_alg_bytes(L: int, m: int, rows) -> float:
+def _batch_alg_bytes(L: int, m: int, rows, df: bool) -> float:
     """Algorithmic HBM bytes of one batched gather launch over quenches sharing one grid: the
-    FP32 weights and int32 starts of the three stencil families and phi2 (FP64) once, plus per
-    quench the FP32 history rows (QK,QR) and (dQK,dQR) the B1/B2 gathers can touch and O(L)
-    row data."""
-    return 3 * L * L * (4 * m + 4) + 8 * L * L + sum(16 * L * n + 64 * L for n in rows)
+    FP32 weights ((hi, lo) planes in the (hi, lo) form) and int32 starts of the three stencil
+    families and phi2 (FP64) once, plus per quench the FP32 history rows the B1/B2 gathers can
+    touch -- (QK, QR), their low parts in the (hi, lo) form, (dQK, dQR) -- and O(L) row data."""
+    w = 8 * m if df else 4 * m
+    per = 24 if df else 16
+    return 3 * L * L * (w + 4) + 8 * L * L + sum(per * L * n + 64 * L for n in rows)
 
 
-def _batch_df(D, torch, args, grid, dev, stream):
-    """The headline workload in the (hi, lo) form (precision mixed_df): same quenches, same
-    setup, `steps` ticks timed."""
+def _batch_other(D, torch, args, grid, dev, stream, precision):
+    """The headline workload in the other mixed form: same quenches, same setup, `steps`
+    ticks timed."""
     B = args.quenches
     cap = args.setup + args.warmup + args.steps + 64
     bt = D.Batch([grid], _batch_quenches(D, B, args.setup, cap), ticks_per_launch=32, device=dev,
-                 stream=stream.cuda_stream, precision="mixed_df")
+                 stream=stream.cuda_stream, precision=precision)
     bt.run(10 ** 9)
     for q in range(B):
         bt.set_limits(q, max_steps=10 ** 12)
@@ -372,7 +383,7 @@ def _mixed_length_batch(D, torch, args, dev, stream):
     cap = args.mixed_length_setup + args.steps + 64
     lengths, qs = mixed_length_quenches(n=args.quenches, capacity=cap, max_steps=args.mixed_length_setup)
     grids = [D.grid.generate(L) for L in lengths]
-    bt = D.Batch(grids, qs, ticks_per_launch=32, device=dev, stream=stream.cuda_stream)
+    bt = D.Batch(grids, qs, ticks_per_launch=32, device=dev, stream=stream.cuda_stream, precision=args.precision)
     bt.run(10 ** 9)
     for q in range(len(qs)):
         bt.set_limits(q, t_stop=qs[q].t_stop, max_steps=10 ** 12)
@@ -489,7 +500,7 @@ def run_ours(args):
     B = args.quenches
     bcap = args.setup + args.warmup + args.steps + 64
     bt = D.Batch([grid], _batch_quenches(D, B, args.setup, bcap), ticks_per_launch=32, device=dev,
-                 stream=stream.cuda_stream)
+                 stream=stream.cuda_stream, precision=args.precision)
     ticks_before = bt.run(10 ** 9)  # untimed: every quench takes `setup` steps from t=0
     for q in range(B):
         bt.set_limits(q, max_steps=10 ** 12)
@@ -526,16 +537,18 @@ def run_ours(args):
 
     if rank != 0:
         return
-    batch_df = _batch_df(D, torch, args, grid, dev, stream) if args.df else None
+    other_prec = "mixed" if args.precision == "mixed_df" else "mixed_df"
+    other = _batch_other(D, torch, args, grid, dev, stream, other_prec) if args.other else None
     mixed_length = _mixed_length_batch(D, torch, args, dev, stream) if args.mixed_length_setup > 0 else None
     adjoint = _adjoint(D, torch, args, dev) if args.adjoint_steps > 0 else None
     # ---- roofline of the dominant kernel: the batched gather, timed live on its stream
     ms_gather = bt.profile(reps=10)
     L, m = args.L, grid.depth
-    alg_bytes = _batch_alg_bytes(L, m, hist)
+    df = args.precision == "mixed_df"
+    alg_bytes = _batch_alg_bytes(L, m, hist, df)
     peaks, src = measured_peaks()
     achieved = alg_bytes / (ms_gather * 1e-3) / 1e9
-    traffic = read_profile_traffic("k_batch_gather_L512.txt")
+    traffic = read_profile_traffic("k_batch_gather_df_L512.txt" if df else "k_batch_gather_L512.txt")
     fp64_peak = probe_fp64(dev)
     fp64_flop = (24 * m + 122) * L * L
     fp64_achieved = fp64_flop / (fp64["stage_ms"]["main"] * 1e-3) / 1e9
@@ -550,8 +563,12 @@ def run_ours(args):
     cfg = _config(args)
     cfg.update({"step": "one tick = one RK stage of every quench", "rk_steps_timed": rk_steps_all,
                 "history_rows": [min(hist), max(hist)], "l2": "inputs > L2 (histories + tables > 1 GB)",
-                "tile": tune or {"threads": 128, "targets": 1}, "precision": "mixed: FP32 gathers/convolutions "
-                "with compensated sums; FP64 r(t), t, C(t,t), error norm",
+                "tile": tune or {"threads": 128, "targets": 1},
+                "precision": ("(hi, lo) mixed: FP32 (hi, lo) weights and history, compensated gathers, "
+                              "double-float stage arithmetic; FP64 r(t), t, C(t,t), error norm; its free "
+                              "controller takes the FP64 form's steps") if df else
+                             "plain mixed: FP32 gathers/convolutions with compensated sums; FP64 r(t), t, "
+                             "C(t,t), error norm",
                 "parallelism": "replicas" if world > 1 else "single GPU"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -562,8 +579,11 @@ def run_ours(args):
                  "k_main_ms": r3(fp64["stage_ms"]["main"]), "k_main_frac_fp64": r3(fp64_achieved / fp64_peak),
                  "fp64_peak_gflops": r3(fp64_peak)},
         "speedup_vs_fp64": r3(value / fp64["value"]),
-        "mixed_df": None if batch_df is None else {"value": r3(batch_df["value"]),
-                                                   "speedup_vs_fp64": r3(batch_df["value"] / fp64["value"])},
+        other_prec: None if other is None else {
+            "value": r3(other["value"]), "speedup_vs_fp64": r3(other["value"] / fp64["value"]),
+            "note": ("plain FP32 gathers: ~1e-7 stage-to-stage rounding noise in the RHS holds its free "
+                     "controller ~1000x below the FP64 step at delta_max 1e-10; steps/s only")
+            if other_prec == "mixed" else "the (hi, lo) form"},
         "mixed_single": None if mixed is None else r3(mixed["value"]),
         "adjoint": None if adjoint is None else {
             "bwd_fwd": r3(adjoint["bwd_fwd_ratio"]), "steps": adjoint["steps"],
@@ -580,8 +600,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None if traffic is None else traffic * B / 64,
                      "frac_dram": None if dram_gbs is None else r3(dram_gbs / peaks["hbm_gbs"]),
-                     "kernel": "k_batch_gather", "ms_per_launch": r3(ms_gather), "peak_source": src,
-                     "note": "alg bytes = tables once + FP32 history rows per quench; L1/issue-bound"},
+                     "kernel": "k_batch_gather" + (" ((hi, lo) form)" if df else ""), "ms_per_launch": r3(ms_gather),
+                     "peak_source": src, "note": "alg bytes = tables once + FP32 history rows per quench; L1-bound"},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "config": cfg,
