@@ -136,24 +136,65 @@ def long_run(grid: Grid, nmax: int, tmax: float, T: float = 0.6, lam: float = 0.
     return out
 
 
+def sparsify_probe(grid: Grid, nsteps: int, T: float = 0.6, lam: float = 0.5,
+                   thresholds=(1e-10, 1e-9, 1e-8, 1e-7)) -> dict:
+    """How many rows one sparsify pass keeps on the same history computed in each form: the
+    FP64 form runs `nsteps` controller steps (no sparsify), the mixed forms replay its
+    schedule; each form's history then goes through one sparsify pass (reference GPU variant)
+    at each threshold, restarting from the unsparsified history every time."""
+    from .simulation import Model, Simulation
+    m = Model(p=3, p2=4, lam=lam, Gamma=T)
+    out = {"form": "sparsify_probe", "L": grid.L, "steps": nsteps, "T": T, "lam": lam, "kept": {}}
+    sched = None
+    for prec in ("fp64", "mixed", "mixed_df"):
+        s = Simulation(grid, m, precision=prec, history_capacity=nsteps + 64)
+        s.init()
+        if sched is None:
+            tr = s.run(nsteps)
+            done = int(np.count_nonzero(tr["dt"]))
+            sched = (tr["dt"][:done], tr["method"][:done])
+            out["t_final"] = float(tr["t"][done - 1])
+        else:
+            s.run(sched[0].size, schedule=sched)
+        st = s.download()
+        out["rows"] = int(st.t1grid.size)
+        kept = {}
+        for thr in thresholds:
+            s.upload(st)
+            kept[f"{thr:g}"] = s.sparsifyNscale(thr)
+        out["kept"][prec] = kept
+        s.close()
+    return out
+
+
+DECADE_FORMS = ("fp64", "mixed", "mixed_df", "fp64_full", "mixed_df_full")
+
+
 def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0.5, every: int = 100000,
-            use_serk2: bool = True, chunk: int = 2000, out_path: str | None = None) -> dict:
-    """One quench in the FP64, mixed and (hi, lo) mixed forms: the FP64 form runs its own
-    controller with the reference GPU loop's periodic block (sparsify every `every` loops,
-    SERK2 climb), the two mixed forms replay its step schedule chunk by chunk with the same
-    cadence (their own sparsify flags).  At every decade t_d = 1, 10, ... up to tmax the run
+            use_serk2: bool = True, chunk: int = 2000, out_path: str | None = None,
+            forms: tuple = ("fp64", "mixed", "mixed_df")) -> dict:
+    """One quench in several forms.  "fp64" runs its own controller with the reference GPU
+    loop's periodic block (sparsify every `every` loops, SERK2 climb); "mixed" and "mixed_df"
+    replay its step schedule chunk by chunk with the same cadence (their own sparsify flags);
+    "fp64_full" and "mixed_df_full" replay it with no sparsify at all, so that their
+    difference is the (hi, lo) form's arithmetic alone and "fp64" against "fp64_full" is what
+    the reference's own sparsify changes.  At every decade t_d = 1, 10, ... up to tmax the run
     stops at the first step reaching t_d and at the first reaching 2 t_d; per form it records
     E(t_d) and r(t_d), R(t_d, t_d/2) = QR of the row at t_d evaluated at theta = (t_d/2)/t, and
     C(2 t_d, t_d) = QK of the row at 2 t_d at theta = t_d/t (a 10-point Lagrange functional of
-    the row, the same on every form); the mixed forms' errors are relative to the FP64 values.
-    Stops early after `wall` seconds; with out_path every finished decade is appended there as
-    one JSON line."""
+    the row, the same on every form).  Errors are relative: a "_full" form against
+    "fp64_full", the other forms against "fp64", and "sparsify_rel_err" is "fp64" against
+    "fp64_full".  Stops early after `wall` seconds; with out_path every finished decade is
+    appended there as one JSON line."""
     import time
     from .grid import lagrange_weights
     from .simulation import Model, Simulation
     m = Model(p=3, p2=4, lam=lam, Gamma=T)
-    names = ("fp64", "mixed", "mixed_df")
-    sims = {k: Simulation(grid, m, precision=k, history_capacity=4096) for k in names}
+    names = ("fp64",) + tuple(f for f in forms if f != "fp64")
+    for f in names:
+        if f not in DECADE_FORMS:
+            raise ValueError(f"unknown form {f}")
+    sims = {k: Simulation(grid, m, precision=k.replace("_full", ""), history_capacity=4096) for k in names}
     for s in sims.values():
         s.init()
     secs = dict.fromkeys(names, 0.0)
@@ -189,7 +230,8 @@ def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0
         for k in names[1:]:
             t0 = time.perf_counter()
             try:
-                res[k] = sims[k].run(done, schedule=sched, **kw)
+                res[k] = sims[k].run(done, schedule=sched,
+                                     **(dict(kw, sparsify_every=0) if k.endswith("_full") else kw))
             except DynError as e:
                 if e.status != DYN_ERR_NONFINITE:
                     raise
@@ -216,7 +258,12 @@ def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0
                 e.setdefault(k, {}).update(vals[k])
             if kind == "C":
                 for k in names[1:]:
-                    e[k + "_rel_err"] = {q: abs(e[k][q] - e["fp64"][q]) / abs(e["fp64"][q]) for q in e["fp64"]}
+                    b = "fp64_full" if k.endswith("_full") and "fp64_full" in names else "fp64"
+                    if k != b:
+                        e[k + "_rel_err"] = {q: abs(e[k][q] - e[b][q]) / abs(e[b][q]) for q in e[b]}
+                if "fp64_full" in names:
+                    e["sparsify_rel_err"] = {q: abs(e["fp64"][q] - e["fp64_full"][q]) / abs(e["fp64_full"][q])
+                                             for q in e["fp64"]}
                 if out_path:
                     with open(out_path, "a") as fh:
                         fh.write(json.dumps(dict(e, seconds=dict(secs), steps=steps)) + "\n")
@@ -229,7 +276,7 @@ def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0
 
 
 def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool = True, chunk: int = 256,
-              max_gb: float = 150.0) -> dict:
+              max_gb: float = 150.0, precision: str = "mixed_df") -> dict:
     """The mixed-L batch run as a whole job: the 64 quenches of mixed_length_quenches (T on
     [0.4, 1.0], lam 0.3/0.5/0.7, L from {256, 512, 1024} and t_stop log-uniform on
     [1e4, 1e7], both drawn from mt19937_64) with every t_stop multiplied by `tscale`, the
@@ -246,11 +293,12 @@ def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool =
     for q in qs:
         q.t_stop *= tscale
         q.capacity = int(1.5 * 424.0 * q.t_stop ** 0.577) + 2048
-        need += q.capacity * lengths[q.grid] * 48.0  # FP64 (QK, QR), (dQK, dQR) + their FP32 mirrors
+        # FP64 (QK, QR), (dQK, dQR) + their FP32 mirrors (+ the low parts of (QK, QR))
+        need += q.capacity * lengths[q.grid] * (56.0 if precision == "mixed_df" else 48.0)
     if need / 1e9 > max_gb:
         raise ValueError(f"batch job needs {need / 1e9:.0f} GB of history, above {max_gb} GB: lower tscale")
     grids = [G.generate(L) for L in lengths]
-    bt = Batch(grids, qs, ticks_per_launch=32, sparsify_every=every, use_serk2=use_serk2)
+    bt = Batch(grids, qs, ticks_per_launch=32, sparsify_every=every, use_serk2=use_serk2, precision=precision)
     t0 = time.perf_counter()
     ticks = bt.run(512)
     tile = bt.tune(reps=3)
@@ -272,7 +320,7 @@ def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool =
     for i in infos:
         status[i["status"]] = status.get(i["status"], 0) + 1
     reached = [i["t"] / q.t_stop for q, i in zip(qs, infos)]
-    return {"form": "batch_job", "quenches": len(qs), "tscale": tscale,
+    return {"form": "batch_job", "precision": precision, "quenches": len(qs), "tscale": tscale,
             "t_stop_range": [min(q.t_stop for q in qs), max(q.t_stop for q in qs)], "sparsify_every": every,
             "use_serk2": use_serk2, "tile": tile, "ticks": ticks, "seconds": sec, "rk_steps": total,
             "steps_per_s": total / sec, "per_L": per_L, "status": status,
@@ -282,16 +330,19 @@ def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool =
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error", "long", "decades", "batch_job"],
+    ap.add_argument("--form", choices=["fp64", "mixed", "batch", "adjoint", "mixed_error", "long", "decades", "batch_job",
+                                       "sparsify_probe"],
                     default="batch")
     ap.add_argument("--wall", type=float, default=600.0, help="decades / batch_job: stop after this many seconds")
     ap.add_argument("--tscale", type=float, default=1e-3, help="batch_job: factor on every stopping time")
     ap.add_argument("--out", default=None, help="decades: append each finished decade to this file")
+    ap.add_argument("--forms", default="fp64,mixed,mixed_df",
+                    help="decades: comma-separated forms out of " + ",".join(DECADE_FORMS))
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--tune", action="store_true", help="batch: autotune the gather tile first")
     ap.add_argument("--tmax", type=float, default=0.0, help="mixed_error: run the FP64 form to t >= tmax")
     ap.add_argument("--precision", choices=["mixed", "mixed_df"], default="mixed",
-                    help="mixed_error / long / fp64 stage timing: the mixed form to compare")
+                    help="mixed_error / long / batch / batch_job / fp64 stage timing: the mixed form")
     ap.add_argument("--L", type=int, default=512)
     ap.add_argument("--rows", type=int, default=4096)
     ap.add_argument("--quenches", type=int, default=16)
@@ -316,10 +367,13 @@ def main(argv=None):
                           "dE_dT": float(g[0]), "dE_dlam": float(g[1]), **stats}))
         return
     if a.form == "batch_job":
-        print(json.dumps(batch_job(a.tscale, a.wall)))
+        print(json.dumps(batch_job(a.tscale, a.wall, precision=a.precision)))
+        return
+    if a.form == "sparsify_probe":
+        print(json.dumps(sparsify_probe(grid, a.steps, a.T)))
         return
     if a.form == "decades":
-        print(json.dumps(decades(grid, a.tmax, a.wall, a.T, out_path=a.out)))
+        print(json.dumps(decades(grid, a.tmax, a.wall, a.T, out_path=a.out, forms=tuple(a.forms.split(",")))))
         return
     if a.form == "long":
         print(json.dumps(long_run(grid, a.steps, a.tmax, a.T, precision=a.precision)))
