@@ -65,8 +65,10 @@ def parse():
     ap.add_argument("--quenches", type=int, default=64)
     ap.add_argument("--no-tune", dest="tune", action="store_false",
                     help="skip the autotuner (dyn_batch_tune) that picks the batched gather tile before timing")
-    ap.add_argument("--mixed-length-setup", type=int, default=1000,
-                    help="untimed steps of every quench of the mixed-L batch before its timed ticks (0: skip it)")
+    ap.add_argument("--mixed-length-tscale", type=float, default=1e-5,
+                    help="mixed-L whole job: factor on every stopping time (0: skip the job)")
+    ap.add_argument("--mixed-length-wall", type=float, default=150.0,
+                    help="mixed-L whole job: stop after this many seconds")
     ap.add_argument("--adjoint-steps", type=int, default=5000, help="FP64 steps of the adjoint measurement (0: skip)")
     ap.add_argument("--precision", choices=["mixed_df", "mixed"], default="mixed_df",
                     help="the headline batch's form: mixed_df, the (hi, lo) form whose step-size controller "
@@ -374,41 +376,19 @@ def _batch_other(D, torch, args, grid, dev, stream, precision):
     return out
 
 
-def _mixed_length_batch(D, torch, args, dev, stream):
-    """The mixed-L batch: 64 quenches, temperatures uniform on [0.4, 1.0], lambda cycling
-    0.3/0.5/0.7, grid length from {256, 512, 1024} and stopping time log-uniform on [1e4, 1e7]
-    drawn from mt19937_64 (fixed seed), mixed precision.  Every quench takes `mixed_length_setup`
-    steps untimed from t=0, then `steps` ticks are timed; value = RK steps completed / time."""
-    from dynamite_gb300.batch import mixed_length_quenches
-    cap = args.mixed_length_setup + args.steps + 64
-    lengths, qs = mixed_length_quenches(n=args.quenches, capacity=cap, max_steps=args.mixed_length_setup)
-    grids = [D.grid.generate(L) for L in lengths]
-    bt = D.Batch(grids, qs, ticks_per_launch=32, device=dev, stream=stream.cuda_stream, precision=args.precision)
-    bt.run(10 ** 9)
-    for q in range(len(qs)):
-        bt.set_limits(q, t_stop=qs[q].t_stop, max_steps=10 ** 12)
-    bt.run(args.warmup)
-    steps0 = bt.total_steps()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+def _mixed_length_job(D, torch, args, dev, stream):
+    """The mixed-L batch run as a whole job: 64 quenches, temperatures uniform on [0.4, 1.0],
+    lambda cycling 0.3/0.5/0.7, grid length from {256, 512, 1024} and stopping time
+    log-uniform on [1e4, 1e7] drawn from mt19937_64 (fixed seed), every stopping time scaled
+    by `mixed_length_tscale`, the batched form of `precision`, the reference GPU loop's
+    periodic block (sparsify every 1e5 loops, SERK2 climb), the autotuned tile; timed from
+    t=0 until every quench has stopped (or `mixed_length_wall` seconds);
+    value = RK steps of all quenches / wall time."""
+    from dynamite_gb300.microbench import batch_job
     torch.cuda.synchronize()
-    e0.record(stream)
-    bt.enqueue(args.steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    bt.sync()
-    t = e0.elapsed_time(e1) / 1e3
-    steps = bt.total_steps() - steps0
-    infos = bt.infos()
-    per_L = {str(L): sum(1 for q in qs if grids[q.grid].L == L) for L in lengths}
-    out = {"value": steps / t, "unit": UNIT, "ticks": args.steps, "rk_steps_timed": steps,
-           "ms_per_tick": 1e3 * t / args.steps, "quenches_per_L": per_L,
-           "t_stop_range": [min(q.t_stop for q in qs), max(q.t_stop for q in qs)],
-           "t_reached_range": [min(i["t"] for i in infos), max(i["t"] for i in infos)],
-           "setup_steps": args.mixed_length_setup,
-           "note": "timed window of the job after the untimed setup; no quench reaches its stopping time "
-                   "inside the window"}
-    bt.close()
-    return out
+    r = batch_job(args.mixed_length_tscale, args.mixed_length_wall, precision=args.precision, device=dev,
+                  stream=stream.cuda_stream)
+    return r
 
 
 def _adjoint(D, torch, args, dev):
@@ -539,7 +519,7 @@ def run_ours(args):
         return
     other_prec = "mixed" if args.precision == "mixed_df" else "mixed_df"
     other = _batch_other(D, torch, args, grid, dev, stream, other_prec) if args.other else None
-    mixed_length = _mixed_length_batch(D, torch, args, dev, stream) if args.mixed_length_setup > 0 else None
+    mixed_length = _mixed_length_job(D, torch, args, dev, stream) if args.mixed_length_tscale > 0 else None
     adjoint = _adjoint(D, torch, args, dev) if args.adjoint_steps > 0 else None
     # ---- roofline of the dominant kernel: the batched gather, timed live on its stream
     ms_gather = bt.profile(reps=10)
@@ -589,9 +569,11 @@ def run_ours(args):
             "bwd_fwd": r3(adjoint["bwd_fwd_ratio"]), "steps": adjoint["steps"],
             "max_rel_err_vs_fd": r3(max(v["rel_err"] for v in adjoint["all_gradients"].values())),
             "peak_gb": r3(adjoint["peak_device_bytes"] / 1e9), "recompute_mismatch": adjoint["recompute_mismatch"]},
-        "mixed_L_batch": None if mixed_length is None else {
-            "value": r3(mixed_length["value"]), "per_L": mixed_length["quenches_per_L"],
-            "t_reached": [r3(x) for x in mixed_length["t_reached_range"]]},
+        "mixed_L_job": None if mixed_length is None else {
+            "value": r3(mixed_length["steps_per_s"]), "seconds": r3(mixed_length["seconds"]),
+            "rk_steps": mixed_length["rk_steps"], "status": mixed_length["status"],
+            "per_L": {k: v["quenches"] for k, v in mixed_length["per_L"].items()},
+            "t_stop": [r3(x) for x in mixed_length["t_stop_range"]], "tscale": args.mixed_length_tscale},
         "e2e": {"value": e2e_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h_tick,
                 "note": "per tick, through dyn_batch_run (32-tick graph replays) + each quench's newest row read "

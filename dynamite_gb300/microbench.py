@@ -276,7 +276,7 @@ def decades(grid: Grid, tmax: float, wall: float, T: float = 0.6, lam: float = 0
 
 
 def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool = True, chunk: int = 256,
-              max_gb: float = 150.0, precision: str = "mixed_df") -> dict:
+              max_gb: float = 150.0, precision: str = "mixed_df", **batch_kw) -> dict:
     """The mixed-L batch run as a whole job: the 64 quenches of mixed_length_quenches (T on
     [0.4, 1.0], lam 0.3/0.5/0.7, L from {256, 512, 1024} and t_stop log-uniform on
     [1e4, 1e7], both drawn from mt19937_64) with every t_stop multiplied by `tscale`, the
@@ -284,7 +284,8 @@ def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool =
     the gather tile the autotuner picks after the first ticks; run until every quench has
     stopped (or `wall` seconds).  History capacity per quench from the step count a quench
     needs to reach its t_stop (about 424 t^0.577 steps for the mixed p-spin at T = 0.6, with
-    a 1.5 margin); the job is refused above `max_gb` of history memory."""
+    a 1.5 margin); the job is refused above `max_gb` of history memory.  `batch_kw` goes to
+    Batch (device, stream)."""
     import time
     from . import grid as G
     from .batch import Batch, mixed_length_quenches
@@ -298,7 +299,8 @@ def batch_job(tscale: float, wall: float, every: int = 100000, use_serk2: bool =
     if need / 1e9 > max_gb:
         raise ValueError(f"batch job needs {need / 1e9:.0f} GB of history, above {max_gb} GB: lower tscale")
     grids = [G.generate(L) for L in lengths]
-    bt = Batch(grids, qs, ticks_per_launch=32, sparsify_every=every, use_serk2=use_serk2, precision=precision)
+    bt = Batch(grids, qs, ticks_per_launch=32, sparsify_every=every, use_serk2=use_serk2, precision=precision,
+               **batch_kw)
     t0 = time.perf_counter()
     ticks = bt.run(512)
     tile = bt.tune(reps=3)
