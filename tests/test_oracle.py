@@ -263,6 +263,25 @@ def test_serk_coefficients_reproduce_the_stability_polynomial(oracle_built, q, t
     assert np.max(np.abs(comb - R) / np.maximum(1.0, np.abs(R))) < tol
 
 
+@pytest.mark.skipif(not O.Reference.available(), reason="reference sources not built here")
+def test_serk_coefficients_equal_reference(oracle_built):
+    """The SERK2(q) weights against SERKcoeffs itself (runge_kutta.cu:228-272), compiled
+    from the reference's CUDA source (host code; `make -C oracle serk`), bit for bit for
+    every q the SERK2 climb reaches.  The library is loaded lazily: runge_kutta.cu's GPU
+    steppers call host functions of files not linked in, and none of them runs."""
+    import ctypes as C
+    import os
+    import subprocess
+    subprocess.run(["make", "-s", "-C", os.path.dirname(O.__file__), "serk"], check=True)
+    lib = C.CDLL(os.path.join(os.path.dirname(O.__file__), "_ref", "libdynref_serk.so"),
+                 mode=os.RTLD_LAZY | os.RTLD_LOCAL)
+    lib.dynref_serk_coeffs.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    for q in range(2, 17, 2):
+        ref = np.empty(2 * q + 1)
+        assert lib.dynref_serk_coeffs(q, ref.ctypes.data_as(C.POINTER(C.c_double))) == 2 * q + 1
+        np.testing.assert_array_equal(O.Port.serk_coeffs(q), ref, err_msg=f"q={q}")
+
+
 def _gpu_variant_numpy(st, L, thr):
     """Variant 2 restated independently in numpy from the reference's CUDA code
     (computeSparsifyFlags and sparsifyNscaleGPU, sparsify_utils.cu:154-290): flags of
