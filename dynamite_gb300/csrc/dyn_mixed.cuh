@@ -602,18 +602,21 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
     return ff_fast(s, e);
 }
 __device__ __forceinline__ ff ff_neg(ff a) { return {-a.h, -a.l}; }
+// Products are left unnormalized: the low word is the exact rounding error of the
+// high product plus the cross terms, at most ~2 ulp of the high word, which every
+// later sum (TwoSum on the high words) and product (cross terms) takes as it is.
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
     const float p = __fmul_rn(a.h, b.h);
     float e = __fmaf_rn(a.h, b.h, -p);
     e = __fmaf_rn(a.h, b.l, e);
     e = __fmaf_rn(a.l, b.h, e);
-    return ff_fast(p, e);
+    return {p, e};
 }
 __device__ __forceinline__ ff ff_mulf(ff a, float b) {
     const float p = __fmul_rn(a.h, b);
     float e = __fmaf_rn(a.h, b, -p);
     e = __fmaf_rn(a.l, b, e);
-    return ff_fast(p, e);
+    return {p, e};
 }
 // q^E as the same left-to-right product chain whether E is a template constant
 // (the specialized models) or a run-time value (the generic kernel): both forms

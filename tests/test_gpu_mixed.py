@@ -124,3 +124,40 @@ def test_df_beyond_the_default_shared_memory(product_built):
     bt.run(1000)
     np.testing.assert_array_equal(bt.download(0).QK, qb)
     bt.close()
+
+
+def test_df_controller_and_sparsify_follow_fp64(product_built):
+    """What makes the (hi, lo) form a free-running replacement for FP64 at delta_max 1e-10
+    (mixed p-spin lam = 0.5, T = 0.6, L = 512, 3000 steps from t = 0): (1) its own
+    step-size controller takes the FP64 form's steps -- its stage derivatives carry no
+    stage-to-stage FP32 rounding noise for the embedded error estimate to read -- and
+    (2) one sparsify pass over the same history keeps FP64's rows.  Both up to
+    decisions that sit within rounding of a threshold: the free runs end within 1e-3 of
+    each other in t (measured 9e-5), and the keep lists may differ in a borderline row
+    (over 4e5 steps at L=512 with four sparsify events: 147,283 rows kept against
+    147,284).  (The plain mixed form meets neither: its free steps stay ~1000x below
+    FP64's and its sparsify keeps far more rows.)"""
+    grid = D.grid.generate(512)
+    m = D.Model(p=3, p2=4, lam=0.5, Gamma=0.6)
+    N = 3000
+    runs, states = {}, {}
+    for prec in ("fp64", "mixed_df"):
+        s = D.Simulation(grid, m, precision=prec, history_capacity=N + 64)
+        s.init()
+        runs[prec] = s.run(N)
+        s.close()
+        assert np.count_nonzero(runs[prec]["dt"]) == N
+    t_fp64 = runs["fp64"]["t"][-1]
+    assert abs(runs["mixed_df"]["t"][-1] - t_fp64) < 1e-3 * t_fp64
+    sched = (runs["fp64"]["dt"], runs["fp64"]["method"])
+    for prec in ("fp64", "mixed_df"):
+        s = D.Simulation(grid, m, precision=prec, history_capacity=N + 64)
+        s.init()
+        s.run(N, schedule=sched)
+        s.sparsifyNscale(1e-10)
+        states[prec] = s.download()
+        s.close()
+    kept, kept_df = states["fp64"].t1grid, states["mixed_df"].t1grid
+    assert kept.size < 0.95 * (N + 1)  # rows were dropped
+    assert abs(kept_df.size - kept.size) <= 2
+    assert np.isin(kept, kept_df).mean() > 0.999
