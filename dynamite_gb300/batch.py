@@ -3,7 +3,9 @@
 The reference runs one quench per process (simulation_runner.cpp:125-304);
 `Batch` advances many quenches together, each with its own model, grid,
 history, step controller (the one `Simulation.run` applies) and stopping rule,
-in the mixed-precision arithmetic of `Simulation(precision="mixed")`.
+in the arithmetic of `Simulation(precision="mixed_df")` (the default: its free
+controller and sparsify decisions match the FP64 form's) or of
+`Simulation(precision="mixed")`.
 
     b = Batch([grid512], [Quench(grid=0, Gamma=0.6, lam=0.5, t_stop=1e4)])
     b.run(max_ticks=10_000)
@@ -52,7 +54,7 @@ class Batch:
     def __init__(self, grids: list[Grid], quenches: list[Quench], search: str = "binary", gpu_rollback: bool = False,
                  ticks_per_launch: int = 32, threads: int = 128, targets: int = 1, ctas_per_sm: int = 0,
                  device: int = 0, stream: int | None = None, sparsify_every: int = 0, sparsify_sweeps: int = -1,
-                 sparsify_variant: str = "gpu", precision: str = "mixed", use_serk2: bool = False):
+                 sparsify_variant: str = "gpu", precision: str = "mixed_df", use_serk2: bool = False):
         self.grids = grids
         self.quenches = list(quenches)
         self._h = C.c_void_p()

@@ -728,10 +728,10 @@ dyn_status dyn_batch_create(const dyn_batch_config* cfg, const dyn_batch_grid* g
             return bfail(DYN_ERR_INVALID, "grid " + std::to_string(g) + ": " + why);
     }
     if (cfg->precision != 0 && cfg->precision != DYN_MIXED && cfg->precision != DYN_MIXED_DF)
-        return bfail(DYN_ERR_INVALID, "batch precision: DYN_MIXED or DYN_MIXED_DF");
+        return bfail(DYN_ERR_INVALID, "batch precision: DYN_MIXED_DF (or 0) or DYN_MIXED");
     Batch* bt = new Batch();
     bt->cfg = *cfg;
-    bt->df = cfg->precision == DYN_MIXED_DF;
+    bt->df = cfg->precision != DYN_MIXED;  // 0 (the default) and DYN_MIXED_DF: the (hi, lo) form
     cudaError_t e = cudaSetDevice(cfg->device);
     if (e != cudaSuccess) { delete bt; return bfail(DYN_ERR_CUDA, cudaGetErrorString(e)); }
     if (cfg->stream) {

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DYN_ABI_VERSION 4
+#define DYN_ABI_VERSION 5
 
 typedef enum {
     DYN_OK = 0,
@@ -405,7 +405,10 @@ typedef struct {
     long long sparsify_every;
     int sparsify_sweeps;
     int sparsify_variant;
-    int precision;           /* DYN_MIXED (or 0) | DYN_MIXED_DF */
+    int precision;           /* DYN_MIXED_DF (or 0) | DYN_MIXED: the (hi, lo) form is the one whose
+                                free step-size controller and sparsify decisions match the FP64
+                                form's at delta_max 1e-10; the plain form's controller reads its
+                                FP32 stage noise as error and keeps the step far smaller */
     int use_serk2;           /* the periodic block's SERK2 climb, as dyn_run_params */
 } dyn_batch_config;
 

@@ -45,7 +45,7 @@ def test_batch_equals_single_quenches(product_built):
     ma = D.Model(p=3, p2=4, lam=0.3, Gamma=0.9)
     mb = D.Model(p=3, p2=4, lam=0.7, Gamma=0.45)
     specs = [(0, m32, 70), (1, ma, 55), (0, mb, 40), (1, m32, 64)]
-    b = D.Batch(grids, [_quench(gi, m, max_steps=n) for gi, m, n in specs], ticks_per_launch=16)
+    b = D.Batch(grids, [_quench(gi, m, max_steps=n) for gi, m, n in specs], ticks_per_launch=16, precision="mixed")
     b.run(100_000)
     for q, (gi, m, n) in enumerate(specs):
         inf = b.info(q)
@@ -62,7 +62,7 @@ def test_batch_generic_exponents(product_built):
     """Quenches with different (p, p2) in one batch take the runtime-exponent kernels."""
     grids, m32, m64 = _grids()
     specs = [(0, m32, 50), (1, m64, 50), (0, D.Model(p=3, p2=0, lam=1.0, Gamma=0.7), 35)]
-    b = D.Batch(grids, [_quench(gi, m, max_steps=n) for gi, m, n in specs])
+    b = D.Batch(grids, [_quench(gi, m, max_steps=n) for gi, m, n in specs], precision="mixed")
     b.run(100_000)
     for q, (gi, m, n) in enumerate(specs):
         s, _ = _single(grids[gi], m, n)
@@ -74,7 +74,7 @@ def test_batch_stopping_time_and_capacity(product_built):
     s, tr = _single(grids[0], m32, 90)
     t_stop = float(tr["t"][60])  # time reached by step 61; the quench stops once t >= t_stop
     b = D.Batch(grids, [_quench(0, m32, t_stop=t_stop), _quench(0, m32, capacity=25),
-                        _quench(1, m32, max_steps=10)])
+                        _quench(1, m32, max_steps=10)], precision="mixed")
     b.run(100_000)
     i0, i1, i2 = b.info(0), b.info(1), b.info(2)
     assert i0["status"] == "done" and i0["t"] >= t_stop
@@ -98,7 +98,8 @@ def test_batch_rollback_matches_single(product_built):
     (simulation_runner.cpp:280-304) against dyn_run's."""
     grids, m32, _ = _grids()
     m = D.Model(p=3, p2=4, lam=0.5, Gamma=0.6, delta_max=1e-13)
-    b = D.Batch(grids, [_quench(0, m, max_steps=80), _quench(1, m, max_steps=60)], gpu_rollback=True)
+    b = D.Batch(grids, [_quench(0, m, max_steps=80), _quench(1, m, max_steps=60)], gpu_rollback=True,
+                precision="mixed")
     b.run(100_000)
     for q, (gi, n) in enumerate([(0, 80), (1, 60)]):
         s, tr = _single(grids[gi], m, n, rollback=True)
@@ -126,7 +127,7 @@ def test_batch_autotuned_tiles(product_built):
     L = 128
     grid = D.grid.generate(L, Tmax=1e3)
     models = [D.Model(p=3, p2=4, lam=lam, Gamma=gm) for lam, gm in ((0.3, 0.5), (0.5, 0.6), (0.7, 0.9))]
-    b = D.Batch([grid], [_quench(0, m, max_steps=40) for m in models])
+    b = D.Batch([grid], [_quench(0, m, max_steps=40) for m in models], precision="mixed")
     b.run(20)  # tune on a live state
     pick = b.tune(reps=3)
     assert pick["threads"] in (128, 256) and pick["targets"] in (1, 2) and pick["ms_gather"] > 0

@@ -68,7 +68,7 @@ def test_overflow_fails_one_batch_quench(product_built):
     grid, m = grid_from(g, D.Grid), model_from(g, D.Model)
     kw = dict(p=m.p, p2=m.p2, lam=m.lam, T0=m.T0, Gamma=m.Gamma, delta_t_min=m.delta_t_min,
               delta_max=m.delta_max, max_steps=6)
-    b = D.Batch([grid], [D.Quench(grid=0, **kw), D.Quench(grid=0, **kw)], ticks_per_launch=8)
+    b = D.Batch([grid], [D.Quench(grid=0, **kw), D.Quench(grid=0, **kw)], ticks_per_launch=8, precision="mixed")
     b.upload(0, _overflowing(g), delta_t=float(g["rk54_dt"][0]), method=1)
     b.run(10_000)
     i0, i1 = b.info(0), b.info(1)

@@ -145,7 +145,7 @@ def test_library_exports_every_declared_symbol(product_built):
     assert len(names) >= 25
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.dyn_abi_version() == 4
+    assert lib.dyn_abi_version() == 5
 
 
 def test_invalid_arguments_rejected_without_touching_the_gpu(product_built):

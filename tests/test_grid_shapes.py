@@ -92,7 +92,7 @@ def test_gpu_forms_on_other_depths(product_built, L, order):
         assert rel_err(c.QK, a.QK) < 1e-6 and rel_err(c.QR, a.QR) < 1e-6, prec
     # batch of two quenches on this grid against the same quenches alone (mixed form)
     qs = [D.Quench(grid=0, p=3, p2=4, lam=lam, Gamma=0.6, max_steps=40, capacity=64) for lam in (0.3, 0.5)]
-    bt = D.Batch([g], qs, ticks_per_launch=16)
+    bt = D.Batch([g], qs, ticks_per_launch=16, precision="mixed")
     bt.run(100_000)
     for q, lam in enumerate((0.3, 0.5)):
         ss = D.Simulation(g, D.Model(p=3, p2=4, lam=lam, Gamma=0.6), precision="mixed")
