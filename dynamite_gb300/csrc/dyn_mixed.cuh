@@ -35,6 +35,24 @@ __device__ __forceinline__ float2 fmul2s(float w, float2 x) {
         : "f"(w), "f"(x.x), "f"(x.y));
     return d;
 }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
 
 template <int E>
 __device__ __forceinline__ float fpow_c(float q) {
@@ -534,6 +552,20 @@ __device__ __forceinline__ float4 gather(const float2* __restrict__ wh, const fl
     return make_float4(sx, cx, sy, cy);
 }
 
+// add_prod for both halves of a (QK, QR) pair at once, in packed FP32x2
+// instructions, each half rounded exactly as add_prod rounds it: -p is formed as
+// (-wh) * xh (round-to-nearest is symmetric), s + p as s - (-p), and p - bp as
+// -((-p) + bp), so every intermediate equals add_prod's up to its sign.
+__device__ __forceinline__ void add_prod2(float2& s, float2& c, float wh, float wl, float2 xh, float2 xl) {
+    const float2 np = fmul2s(-wh, xh);
+    float2 e = ffma2s(wh, xh, np);
+    e = ffma2s(wh, xl, e);
+    e = ffma2s(wl, xh, e);
+    const float2 t = fsub2(s, np), bp = fsub2(t, s);
+    c = fadd2(c, fadd2(fsub2(fsub2(s, fsub2(t, bp)), fadd2(np, bp)), e));
+    s = t;
+}
+
 // The depth-10 gather with the (hi, lo) history read as six 16-byte loads per
 // array from the even element at or below the start b (the seg10 layout),
 // weights wh/wl already in registers; taps in order.
@@ -544,7 +576,7 @@ __device__ __forceinline__ float4 gather10(const float wh[10], const float wl[10
     const bool sh = b & 1;
     const float4* ph = reinterpret_cast<const float4*>(xh + a);
     const float4* pl = reinterpret_cast<const float4*>(xl + a);
-    float sx = 0.f, cx = 0.f, sy = 0.f, cy = 0.f;
+    float2 s = make_float2(0.f, 0.f), c = make_float2(0.f, 0.f);
     float2 hprev = make_float2(0.f, 0.f), lprev = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
@@ -555,20 +587,16 @@ __device__ __forceinline__ float4 gather10(const float wh[10], const float wl[10
         const float2 l0 = make_float2(vl.x, vl.y), l1 = make_float2(vl.z, vl.w);
         if (k >= 1) {
             const int d = 2 * k - 1;
-            const float2 xh_ = sh ? h0 : hprev, xl_ = sh ? l0 : lprev;
-            add_prod(sx, cx, wh[d], wl[d], xh_.x, xl_.x);
-            add_prod(sy, cy, wh[d], wl[d], xh_.y, xl_.y);
+            add_prod2(s, c, wh[d], wl[d], sh ? h0 : hprev, sh ? l0 : lprev);
         }
         if (k <= 4) {
             const int d = 2 * k;
-            const float2 xh_ = sh ? h1 : h0, xl_ = sh ? l1 : l0;
-            add_prod(sx, cx, wh[d], wl[d], xh_.x, xl_.x);
-            add_prod(sy, cy, wh[d], wl[d], xh_.y, xl_.y);
+            add_prod2(s, c, wh[d], wl[d], sh ? h1 : h0, sh ? l1 : l0);
         }
         hprev = h1;
         lprev = l1;
     }
-    return make_float4(sx, cx, sy, cy);
+    return make_float4(s.x, c.x, s.y, c.y);
 }
 
 __device__ __forceinline__ void load_w10_hl(const float2* __restrict__ wh, const float2* __restrict__ wl, size_t L2,
