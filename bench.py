@@ -583,7 +583,9 @@ def run_ours(args):
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None if traffic is None else traffic * B / 64,
                      "frac_dram": None if dram_gbs is None else r3(dram_gbs / peaks["hbm_gbs"]),
                      "kernel": "k_batch_gather" + (" ((hi, lo) form)" if df else ""), "ms_per_launch": r3(ms_gather),
-                     "peak_source": src, "note": "alg bytes = tables once + FP32 history rows per quench; L1-bound"},
+                     "peak_source": src,
+                     "note": "alg bytes = tables once + the FP32 history rows per quench; "
+                             + ("latency-bound (long-scoreboard stalls at 50 % occupancy)" if df else "L1-bound")},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "config": cfg,
