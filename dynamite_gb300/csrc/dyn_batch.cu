@@ -476,7 +476,24 @@ struct Batch {
             cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return 1;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, threads, smem) != cudaSuccess) return 1;
-        return nb > 0 ? nb : 1;
+        nb = nb > 0 ? nb : 1;
+        // ask for the smallest shared-memory carveout that still holds nb CTAs, so the rest
+        // of the SM's unified 256 KB stays L1 for the gathers' history lines and spills
+        cudaFuncAttributes fa;
+        int dev = 0, smem_sm = 0, reserved = 0;
+        if (cudaFuncGetAttributes(&fa, f) == cudaSuccess && cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess &&
+            smem_sm > 0) {
+            const size_t need = (size_t)nb * (fa.sharedSizeBytes + smem + (size_t)reserved);
+            const int pct = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / smem_sm);
+            cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+            int nb2 = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, f, threads, smem) == cudaSuccess && nb2 < nb)
+                cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, -1);  // keep nb resident
+        }
+        cudaGetLastError();  // a refused hint is not an error of the batch
+        return nb;
     }
 
     dyn_status set_tile(int threads, int targets, int ctas_per_sm) {

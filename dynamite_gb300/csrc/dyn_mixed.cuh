@@ -267,7 +267,7 @@ __device__ __forceinline__ void split_at(const ListView& L, const float* __restr
 
 
 // Block-shared scratch of one target row
-constexpr int RED_CAP = 512;  // per-warp partial sums held between folds (doubles)
+constexpr int RED_CAP = 256;  // per-warp partial sums held between folds (float pairs)
 constexpr int MAX_SEG = 4096 / 32;  // 32-target segments of the longest row
 struct RowShared {
     int seg[MAX_SEG + 1];  // B2 interval brackets: seg[w] = k(phi2[i][32 w] t), seg[nseg] = k(phi2[i][L-1] t)
