@@ -599,6 +599,17 @@ __device__ __forceinline__ float4 gather10(const float wh[10], const float wl[10
     return make_float4(s.x, c.x, s.y, c.y);
 }
 
+// The depth-10 gather of the staged newest row in shared memory, read tap by tap
+// (8-byte loads at any offset, no parity selects); taps in the same order as
+// gather10, so the two give the same sums
+__device__ __forceinline__ float4 gather10_staged(const float wh[10], const float wl[10], const float2* xh,
+                                                  const float2* xl) {
+    float2 s = make_float2(0.f, 0.f), c = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 10; ++d) add_prod2(s, c, wh[d], wl[d], xh[d], xl[d]);
+    return make_float4(s.x, c.x, s.y, c.y);
+}
+
 __device__ __forceinline__ void load_w10_hl(const float2* __restrict__ wh, const float2* __restrict__ wl, size_t L2,
                                             size_t ij, float h[10], float l[10]) {
 #pragma unroll
@@ -722,9 +733,9 @@ __device__ __forceinline__ void chunk_dd(const DevCtx& c, const StageDev& sp, co
                     if constexpr (M == 10) {
                         float wh[10], wl[10];
                         load_w10_hl(c.wA1f, c.wA1l, L2, ij, wh, wl);
-                        g1 = gather10<false>(wh, wl, s_hi, s_lo, (size_t)s1);
+                        g1 = gather10_staged(wh, wl, s_hi + s1, s_lo + s1);
                         load_w10_hl(c.wA2f, c.wA2l, L2, ij, wh, wl);
-                        g2 = gather10<false>(wh, wl, s_hi, s_lo, (size_t)s2);
+                        g2 = gather10_staged(wh, wl, s_hi + s2, s_lo + s2);
                     } else {
                         g1 = gather<M>(c.wA1f, c.wA1l, L2, ij, s_hi + s1, s_lo + s1, m, false);
                         g2 = gather<M>(c.wA2f, c.wA2l, L2, ij, s_hi + s2, s_lo + s2, m, false);
