@@ -566,48 +566,31 @@ __device__ __forceinline__ void add_prod2(float2& s, float2& c, float wh, float 
     s = t;
 }
 
-// The depth-10 gather with the (hi, lo) history read as six 16-byte loads per
-// array from the even element at or below the start b (the seg10 layout),
-// weights wh/wl already in registers; taps in order.
-template <bool LDG>
-__device__ __forceinline__ float4 gather10(const float wh[10], const float wl[10], const float2* xh, const float2* xl,
-                                           size_t b) {
-    const size_t a = b & ~(size_t)1;
-    const bool sh = b & 1;
-    const float4* ph = reinterpret_cast<const float4*>(xh + a);
-    const float4* pl = reinterpret_cast<const float4*>(xl + a);
-    float2 s = make_float2(0.f, 0.f), c = make_float2(0.f, 0.f);
-    float2 hprev = make_float2(0.f, 0.f), lprev = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const float4 vh = LDG ? __ldg(ph + k) : ph[k];
-        const float4 vl = LDG ? __ldg(pl + k) : pl[k];
-        // elements 2k, 2k+1 of the window; tap d reads element d + (b & 1)
-        const float2 h0 = make_float2(vh.x, vh.y), h1 = make_float2(vh.z, vh.w);
-        const float2 l0 = make_float2(vl.x, vl.y), l1 = make_float2(vl.z, vl.w);
-        if (k >= 1) {
-            const int d = 2 * k - 1;
-            add_prod2(s, c, wh[d], wl[d], sh ? h0 : hprev, sh ? l0 : lprev);
-        }
-        if (k <= 4) {
-            const int d = 2 * k;
-            add_prod2(s, c, wh[d], wl[d], sh ? h1 : h0, sh ? l1 : l0);
-        }
-        hprev = h1;
-        lprev = l1;
-    }
-    return make_float4(s.x, c.x, s.y, c.y);
-}
-
-// The depth-10 gather of the staged newest row in shared memory, read tap by tap
-// (8-byte loads at any offset, no parity selects); taps in the same order as
-// gather10, so the two give the same sums
+// The depth-10 (hi, lo) gathers, read tap by tap (8-byte loads at any offset:
+// no aligned 16-byte window and no per-tap parity selects), taps in order.  Of
+// the staged newest row in shared memory:
 __device__ __forceinline__ float4 gather10_staged(const float wh[10], const float wl[10], const float2* xh,
                                                   const float2* xl) {
     float2 s = make_float2(0.f, 0.f), c = make_float2(0.f, 0.f);
 #pragma unroll
     for (int d = 0; d < 10; ++d) add_prod2(s, c, wh[d], wl[d], xh[d], xl[d]);
     return make_float4(s.x, c.x, s.y, c.y);
+}
+
+// of a history segment in global memory (read-only path):
+__device__ __forceinline__ float4 gather10_ldg(const float wh[10], const float wl[10], const float2* __restrict__ xh,
+                                               const float2* __restrict__ xl) {
+    float2 s = make_float2(0.f, 0.f), c = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 10; ++d) add_prod2(s, c, wh[d], wl[d], __ldg(xh + d), __ldg(xl + d));
+    return make_float4(s.x, c.x, s.y, c.y);
+}
+// and the FP32 sum of a derivative-row segment with the high weights:
+__device__ __forceinline__ float2 dot10_ldg(const float w[10], const float2* __restrict__ x) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 10; ++d) acc = ffma2s(w[d], __ldg(x + d), acc);
+    return acc;
 }
 
 __device__ __forceinline__ void load_w10_hl(const float2* __restrict__ wh, const float2* __restrict__ wl, size_t L2,
@@ -781,13 +764,13 @@ __device__ __forceinline__ void chunk_dd(const DevCtx& c, const StageDev& sp, co
                     float4 S0, S1;
                     float2 D1, D2 = make_float2(0.f, 0.f);
                     if constexpr (M == 10) {
-                        // even L (the M == 10 kernels require it): every row segment has base's parity
+                        // one weight load for the four segments of rows X-1, X, X+1
                         float wh[10], wl[10];
                         load_w10_hl(c.wB2f, c.wB2l, L2, ij, wh, wl);
-                        S0 = gather10<true>(wh, wl, c.KRf, c.KRl, base);
-                        S1 = gather10<true>(wh, wl, c.KRf, c.KRl, base + L);
-                        D1 = seg10(wh, c.dKRf, base + L);
-                        if (cubic2) D2 = seg10(wh, c.dKRf, base + 2 * L);
+                        S0 = gather10_ldg(wh, wl, c.KRf + base, c.KRl + base);
+                        S1 = gather10_ldg(wh, wl, c.KRf + base + L, c.KRl + base + L);
+                        D1 = dot10_ldg(wh, c.dKRf + base + L);
+                        if (cubic2) D2 = dot10_ldg(wh, c.dKRf + base + 2 * L);
                     } else {
                         S0 = gather<M>(c.wB2f, c.wB2l, L2, ij, c.KRf + base, c.KRl + base, m, true);
                         S1 = gather<M>(c.wB2f, c.wB2l, L2, ij, c.KRf + base + L, c.KRl + base + L, m, true);
