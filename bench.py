@@ -572,7 +572,7 @@ def run_ours(args):
         "mixed_L_job": None if mixed_length is None else {
             "value": r3(mixed_length["steps_per_s"]), "seconds": r3(mixed_length["seconds"]),
             "rk_steps": mixed_length["rk_steps"], "status": mixed_length["status"],
-            "per_L": {k: v["quenches"] for k, v in mixed_length["per_L"].items()},
+            "per_L": {k: v["quenches"] for k, v in mixed_length["per_L"].items()}, "tile": mixed_length["tile"],
             "t_stop": [r3(x) for x in mixed_length["t_stop_range"]], "tscale": args.mixed_length_tscale},
         "e2e": {"value": e2e_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": d2h_tick,
