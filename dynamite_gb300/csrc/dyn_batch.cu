@@ -478,7 +478,10 @@ struct Batch {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, threads, smem) != cudaSuccess) return 1;
         nb = nb > 0 ? nb : 1;
         // ask for the smallest shared-memory carveout that still holds nb CTAs, so the rest
-        // of the SM's unified 256 KB stays L1 for the gathers' history lines and spills
+        // of the SM's unified 256 KB stays L1 for the gathers' history lines and spills.  The
+        // hint belongs to the kernel, not to this batch: of two live batches with different
+        // row lengths the later tile setting decides, and a batch whose CTAs then do not all
+        // fit at once runs them in waves (no CTA of the gather waits on another).
         cudaFuncAttributes fa;
         int dev = 0, smem_sm = 0, reserved = 0;
         if (cudaFuncGetAttributes(&fa, f) == cudaSuccess && cudaGetDevice(&dev) == cudaSuccess &&
