@@ -252,8 +252,8 @@ __device__ void adapt_step(const Quench& q, Plan& pl, const TabDev& tb) {
 #endif
 // DF: the (hi, lo) form (mdf::chunk_dd): twice the staged row and a double-float
 // tail; a cap of 64 registers (DYN_BATCH_DF_TPSM = 1024 threads per SM) spills a
-// little but measured best for 64 quenches at L=512: 1.92 ms against 2.02 (56
-// registers), 1.98 (72) and 2.15 (80).
+// little but measures best for 64 quenches at L=512: 1.55 ms against 1.62 (56
+// registers), 1.61 (72) and 1.74 (80).
 template <int M, int K, int P, int P2, int TPB, bool DF = false>
 __global__ void __launch_bounds__(TPB, DF ? DYN_BATCH_DF_TPSM / TPB : (K == 1 ? DYN_BATCH_TPSM : 512) / TPB)
     k_batch_gather(const Quench* __restrict__ Q, const Plan* __restrict__ PL, const unsigned* __restrict__ items,
